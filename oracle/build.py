@@ -1,0 +1,65 @@
+"""Build recipe for the test oracle -- TEST INFRASTRUCTURE ONLY.
+
+* ``oracle/_build/liboracle.so``: the C++ restatement (prbf_oracle.cpp), built on every
+  machine (plain g++, OpenMP, -ffp-contract=off so expressions round as written).
+* ``oracle/_ref/libref2d.so`` / ``libref3d.so``: the reference's own 2d/ and 3d/ sources
+  (get_cluster.h, get_trunc.h, get_buffer.h, get_vorticity.h, matmult.cxx,
+  mpi_range.cxx) compiled unmodified where they lie, against the sequential PETSc/MPI
+  stand-in in ``oracle/ref_stub``. Only built where the reference tree is present; it
+  generates the golden fixtures under tests/golden and is never shipped or linked by
+  the product.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _stale(out, srcs):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_oracle(force=False):
+    out = os.path.join(HERE, "_build", "liboracle.so")
+    srcs = [os.path.join(HERE, "prbf_oracle.cpp"), os.path.join(HERE, "prbf_oracle.h")]
+    if force or _stale(out, srcs):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        _run(["g++"] + CXXFLAGS + ["-o", out, srcs[0]])
+    return out
+
+
+def build_ref(ref_root, force=False):
+    """Compile the reference's own sources (read in place) into oracle/_ref."""
+    outs = []
+    stub = os.path.join(HERE, "ref_stub")
+    for dim in (2, 3):
+        tree = os.path.join(ref_root, "%dd" % dim)
+        if not os.path.isdir(tree):
+            continue
+        out = os.path.join(HERE, "_ref", "libref%dd.so" % dim)
+        srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(tree, "matmult.cxx"),
+                os.path.join(tree, "mpi_range.cxx")]
+        deps = srcs + [os.path.join(stub, "petscksp.h"), os.path.join(stub, "mpi.h")]
+        if force or _stale(out, deps):
+            os.makedirs(os.path.dirname(out), exist_ok=True)
+            _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+                  "-DREF_DIM=%d" % dim, "-I", stub, "-I", tree, "-o", out] + srcs)
+        outs.append(out)
+    return outs
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="-f" in sys.argv))
+    if len(sys.argv) > 1 and os.path.isdir(sys.argv[-1]):
+        print(build_ref(sys.argv[-1], force="-f" in sys.argv))

@@ -1,0 +1,666 @@
+/*
+ * prbf_oracle.cpp -- TEST INFRASTRUCTURE ONLY (checker and timed CPU baseline).
+ *
+ * Plain C++ restatement of PetRBF's solve path. Every function names the reference
+ * file:line (paths inside the petrbf project) that it restates. Built with
+ * -ffp-contract=off so that each floating-point expression is evaluated exactly as
+ * written in the reference (no fused multiply-add), which makes cell membership and
+ * the truncation/buffer box tests bit-reproducible.
+ *
+ * Not product code: only tests/, bench.py (cpu_baseline / --impl reference) and
+ * __graft_entry__.smoke() load this library, and only as the checker.
+ */
+#include "prbf_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double kEpsf = 1e-6;  // 2d/par.h:153
+
+enum {
+  OK = 0,
+  ERR_ARG = 1,
+  ERR_RANGE = 2,
+  ERR_SINGULAR = 3,
+};
+
+// PETSc KSPConvergedReason values used for the solve status.
+enum {
+  CONVERGED_RTOL = 2,
+  CONVERGED_ATOL = 3,
+  DIVERGED_ITS = -3,
+  DIVERGED_DTOL = -4,
+  DIVERGED_BREAKDOWN = -5,
+  DIVERGED_NANORINF = -9,
+};
+
+inline void cell_coords(const orc_grid* g, int ic, int* ix, int* iy, int* iz) {
+  if (g->dim == 2) {
+    *ix = ic / g->ny;
+    *iy = ic % g->ny;
+    *iz = 0;
+  } else {
+    int nxy = g->nx * g->ny;
+    *iz = ic / nxy;
+    int rem = ic % nxy;
+    *ix = rem / g->ny;
+    *iy = rem % g->ny;
+  }
+}
+
+// Cell linear index: 2d/get_cluster.h:80 (ix*ny+iy), 3d/get_cluster.h:101 (iz*nx*ny+ix*ny+iy).
+inline int cell_index(const orc_grid* g, int ix, int iy, int iz) {
+  if (g->dim == 2) return ix * g->ny + iy;
+  return iz * g->nx * g->ny + ix * g->ny + iy;
+}
+
+// Cell centre: 2d/get_cluster.h:217-218, 3d/get_cluster.h:79-81.
+inline void cell_centre(const orc_grid* g, int ix, int iy, int iz, double* xc, double* yc,
+                        double* zc) {
+  *xc = g->xmin + (ix + 0.5) * g->box;
+  *yc = g->ymin + (iy + 0.5) * g->box;
+  *zc = g->dim == 3 ? g->zmin + (iz + 0.5) * g->box : 0.0;
+}
+
+inline int point_cell(const orc_grid* g, double x, double y, double z) {
+  // 2d/get_cluster.h:234-236 ; 3d/get_cluster.h:98-101
+  int ix = (int)floor((x - g->xmin) / g->box);
+  int iy = (int)floor((y - g->ymin) / g->box);
+  int iz = 0;
+  if (g->dim == 3) iz = (int)floor((z - g->zmin) / g->box);
+  if (ix < 0 || ix >= g->nx || iy < 0 || iy >= g->ny || iz < 0 ||
+      (g->dim == 3 && iz >= g->nz))
+    return -1;
+  return cell_index(g, ix, iy, iz);
+}
+
+// Neighbour-cell walk shared by get_trunc and get_buffer: centre first, then the
+// neighbour cells in jx, jy (, jz) order, skipping the centre
+// (2d/get_trunc.h:23-73, 2d/get_buffer.h:13-77, 3d twins).
+template <class F>
+void walk_neighbours(const orc_grid* g, int ic, int nb, F&& visit_cell) {
+  int ix, iy, iz;
+  cell_coords(g, ic, &ix, &iy, &iz);
+  int jx0 = std::max(0, ix - nb), jx1 = std::min(g->nx - 1, ix + nb);
+  int jy0 = std::max(0, iy - nb), jy1 = std::min(g->ny - 1, iy + nb);
+  int jz0 = 0, jz1 = 0;
+  if (g->dim == 3) {
+    jz0 = std::max(0, iz - nb);
+    jz1 = std::min(g->nz - 1, iz + nb);
+  }
+  for (int jx = jx0; jx <= jx1; jx++)
+    for (int jy = jy0; jy <= jy1; jy++)
+      for (int jz = jz0; jz <= jz1; jz++) {
+        if (g->dim == 2) {
+          if (ix != jx || iy != jy) visit_cell(cell_index(g, jx, jy, 0));
+        } else {
+          if (ix != jx || iy != jy || iz != jz) visit_cell(cell_index(g, jx, jy, jz));
+        }
+      }
+}
+
+// Truncation set of target cell ic as indices into the sorted source arrays
+// (2d/get_trunc.h:9-78; 3d/get_trunc.h:9-90).
+int trunc_set(const orc_grid* g, int ic, const double* sx, const double* sy,
+              const double* sz, const int* cs_src, const int* cs_tgt, int* out) {
+  if (cs_tgt[ic] >= cs_tgt[ic + 1]) return 0;  // empty target cell: nptruncj = 0
+  int ix, iy, iz;
+  cell_coords(g, ic, &ix, &iy, &iz);
+  double xc, yc, zc;
+  cell_centre(g, ix, iy, iz, &xc, &yc, &zc);
+  int n = 0;
+  for (int j = cs_src[ic]; j < cs_src[ic + 1]; j++) {
+    if (out) out[n] = j;
+    n++;
+  }
+  const double L = g->trunc_len;
+  walk_neighbours(g, ic, g->nb_trunc, [&](int jc) {
+    for (int j = cs_src[jc]; j < cs_src[jc + 1]; j++) {
+      bool in = fabs(sx[j] - xc) < L && fabs(sy[j] - yc) < L;
+      if (g->dim == 3) in = in && fabs(sz[j] - zc) < L;
+      if (in) {
+        if (out) out[n] = j;
+        n++;
+      }
+    }
+  });
+  return n;
+}
+
+// Buffer (RASM subdomain) of cell ic, centre points first (2d/get_buffer.h:9-77).
+int buffer_set(const orc_grid* g, int ic, const double* x, const double* y, const double* z,
+               const int* cs, int* out) {
+  if (cs[ic] >= cs[ic + 1]) return 0;
+  int ix, iy, iz;
+  cell_coords(g, ic, &ix, &iy, &iz);
+  double xc, yc, zc;
+  cell_centre(g, ix, iy, iz, &xc, &yc, &zc);
+  int n = 0;
+  for (int j = cs[ic]; j < cs[ic + 1]; j++) {
+    if (out) out[n] = j;
+    n++;
+  }
+  const double L = g->buffer_len;
+  walk_neighbours(g, ic, g->nb_buffer, [&](int jc) {
+    for (int j = cs[jc]; j < cs[jc + 1]; j++) {
+      bool in = fabs(x[j] - xc) < L && fabs(y[j] - yc) < L;
+      if (g->dim == 3) in = in && fabs(z[j] - zc) < L;
+      if (in) {
+        if (out) out[n] = j;
+        n++;
+      }
+    }
+  });
+  return n;
+}
+
+// Kernel entry phi(|xi-xj|) exactly as written in 2d/matmult.cxx:39-40 / 83-93
+// (3d/matmult.cxx:40-41): exp(-r^2/(2 sigma^2)) / (2 pi sigma^2), 2D normalisation in 3D.
+inline double phi(double sigma, double dx, double dy, double dz, int dim) {
+  double r2 = dim == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
+  return exp(-(r2) / (2 * sigma * sigma)) / (2 * M_PI * sigma * sigma);
+}
+
+// Deterministic sum: fixed 256 chunks summed in order, independent of thread count.
+double det_dot(int n, const double* a, const double* b) {
+  const int nch = 256;
+  double part[nch];
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nch; c++) {
+    long long lo = (long long)n * c / nch, hi = (long long)n * (c + 1) / nch;
+    double s = 0;
+    for (long long i = lo; i < hi; i++) s += a[i] * b[i];
+    part[c] = s;
+  }
+  double s = 0;
+  for (int c = 0; c < nch; c++) s += part[c];
+  return s;
+}
+
+struct Rasm {
+  int n = 0;
+  int ncell = 0;
+  std::vector<int> cs;                // cell starts (sorted order)
+  std::vector<long long> off;         // buffer list offsets
+  std::vector<int> idx;               // buffer lists
+  std::vector<long long> aoff;        // factor offsets (nb*nb each)
+  std::vector<double> lu;             // LU factors (row-major)
+  std::vector<int> piv;               // pivot rows, per block (offset = off)
+};
+
+// Dense LU with partial pivoting (row interchanges), the algorithm PETSc's
+// -sub_pc_type lu uses for -sub_mat_type dense (LAPACK getrf semantics).
+int lu_factor(int n, double* A, int* piv) {
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    double amax = fabs(A[(size_t)k * n + k]);
+    for (int i = k + 1; i < n; i++) {
+      double v = fabs(A[(size_t)i * n + k]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    piv[k] = p;
+    if (amax == 0.0) return ERR_SINGULAR;
+    if (p != k) {
+      for (int j = 0; j < n; j++) std::swap(A[(size_t)k * n + j], A[(size_t)p * n + j]);
+    }
+    double inv = 1.0 / A[(size_t)k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      double* ri = A + (size_t)i * n;
+      double l = ri[k] * inv;
+      ri[k] = l;
+      if (l != 0.0) {
+        const double* rk = A + (size_t)k * n;
+        for (int j = k + 1; j < n; j++) ri[j] -= l * rk[j];
+      }
+    }
+  }
+  return OK;
+}
+
+void lu_solve(int n, const double* A, const int* piv, double* b) {
+  for (int k = 0; k < n; k++) {
+    if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+  }
+  for (int i = 0; i < n; i++) {
+    const double* ri = A + (size_t)i * n;
+    double s = b[i];
+    for (int j = 0; j < i; j++) s -= ri[j] * b[j];
+    b[i] = s;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    const double* ri = A + (size_t)i * n;
+    double s = b[i];
+    for (int j = i + 1; j < n; j++) s -= ri[j] * b[j];
+    b[i] = s / ri[i];
+  }
+}
+
+void gauss_sum_impl(const orc_grid* g, const double* tx, const double* ty, const double* tz,
+                    const int* cs_tgt, const double* sx, const double* sy, const double* sz,
+                    const double* sg, const int* cs_src, double* w) {
+#pragma omp parallel
+  {
+    std::vector<int> list;
+#pragma omp for schedule(dynamic, 4)
+    for (int ic = 0; ic < g->ncell; ic++) {
+      if (cs_tgt[ic] >= cs_tgt[ic + 1]) continue;
+      int cnt = trunc_set(g, ic, sx, sy, sz, cs_src, cs_tgt, nullptr);
+      list.resize(std::max<size_t>(list.size(), (size_t)cnt));
+      trunc_set(g, ic, sx, sy, sz, cs_src, cs_tgt, list.data());
+      // 2d/matmult.cxx:33-43 (3d/matmult.cxx:33-44)
+      for (int i = cs_tgt[ic]; i < cs_tgt[ic + 1]; i++) {
+        double acc = 0;
+        for (int t = 0; t < cnt; t++) {
+          int j = list[t];
+          double dx = tx[i] - sx[j];
+          double dy = ty[i] - sy[j];
+          // same grouping as the reference: (g * exp(.)) / (2 pi sigma^2)
+          double r2 = g->dim == 3 ? dx * dx + dy * dy + (tz[i] - sz[j]) * (tz[i] - sz[j])
+                                  : dx * dx + dy * dy;
+          acc += sg[j] * exp(-(r2) / (2 * g->sigma * g->sigma)) /
+                 (2 * M_PI * g->sigma * g->sigma);
+        }
+        w[i] = acc;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// 2d/get_cluster.h:176-190 ; 3d/get_cluster.h:21-44 ; widths: 2d/get_trunc.h:14, 2d/get_buffer.h:11
+int orc_grid_make(int dim, double pxmin, double pxmax, double pymin, double pymax,
+                  double pzmin, double pzmax, double sigma, int nsigma_box,
+                  int sigma_buffer, int sigma_trunc, orc_grid* g) {
+  if (!g || (dim != 2 && dim != 3) || !(sigma > 0) || nsigma_box <= 0) return ERR_ARG;
+  memset(g, 0, sizeof(*g));
+  g->dim = dim;
+  g->sigma = sigma;
+  g->nsigma_box = nsigma_box;
+  g->sigma_buffer = sigma_buffer;
+  g->sigma_trunc = sigma_trunc;
+  g->nb_buffer = (int)ceil((sigma_buffer - nsigma_box + kEpsf) / 2 / nsigma_box);
+  g->nb_trunc = (int)ceil((sigma_trunc - nsigma_box + kEpsf) / 2 / nsigma_box);
+  if (g->nb_buffer < 0) g->nb_buffer = 0;
+  if (g->nb_trunc < 0) g->nb_trunc = 0;
+  double xmin = pxmin - kEpsf, xmax = pxmax + kEpsf;
+  double ymin = pymin - kEpsf, ymax = pymax + kEpsf;
+  double zmin = pzmin - kEpsf, zmax = pzmax + kEpsf;
+  g->xmin = xmin;
+  g->ymin = ymin;
+  g->zmin = dim == 3 ? zmin : 0.0;
+  g->box = nsigma_box * sigma + kEpsf;
+  g->nx = (int)ceil((xmax - xmin) / g->box);
+  g->ny = (int)ceil((ymax - ymin) / g->box);
+  g->nz = dim == 3 ? (int)ceil((zmax - zmin) / g->box) : 1;
+  long long nc = (long long)g->nx * g->ny * g->nz;
+  if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || nc > (1LL << 30)) return ERR_RANGE;
+  g->ncell = (int)nc;
+  g->trunc_len = sigma_trunc * sigma / 2 + kEpsf;
+  g->buffer_len = sigma_buffer * sigma / 2 + kEpsf;
+  return OK;
+}
+
+int orc_cell_ids(const orc_grid* g, int n, const double* x, const double* y, const double* z,
+                 int* cell) {
+  int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+  for (int i = 0; i < n; i++) {
+    cell[i] = point_cell(g, x[i], y[i], g->dim == 3 ? z[i] : 0.0);
+    if (cell[i] < 0) bad = 1;
+  }
+  return bad ? ERR_RANGE : OK;
+}
+
+// Stable counting sort by cell (2d/get_cluster.h:233-264 counts and offsets,
+// 2d/get_cluster.h:279-286 sorted-slot writes in ascending original index).
+int orc_cell_sort(const orc_grid* g, int n, const double* x, const double* y, const double* z,
+                  int* perm, int* cell_start) {
+  std::vector<int> cell(n);
+  int st = orc_cell_ids(g, n, x, y, z, cell.data());
+  if (st) return st;
+  std::vector<int> cnt(g->ncell + 1, 0);
+  for (int i = 0; i < n; i++) cnt[cell[i]]++;
+  cell_start[0] = 0;
+  for (int c = 0; c < g->ncell; c++) cell_start[c + 1] = cell_start[c] + cnt[c];
+  std::vector<int> pos(cell_start, cell_start + g->ncell);
+  for (int i = 0; i < n; i++) perm[pos[cell[i]]++] = i;
+  return OK;
+}
+
+int orc_trunc_counts(const orc_grid* g, const double* sx, const double* sy, const double* sz,
+                     const int* cs_src, const int* cs_tgt, int* counts) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int ic = 0; ic < g->ncell; ic++)
+    counts[ic] = trunc_set(g, ic, sx, sy, sz, cs_src, cs_tgt, nullptr);
+  return OK;
+}
+
+int orc_trunc_list(const orc_grid* g, int cell, const double* sx, const double* sy,
+                   const double* sz, const int* cs_src, const int* cs_tgt, int* idx) {
+  if (cell < 0 || cell >= g->ncell) return -1;
+  return trunc_set(g, cell, sx, sy, sz, cs_src, cs_tgt, idx);
+}
+
+int orc_gauss_sum(const orc_grid* g, const double* tx, const double* ty, const double* tz,
+                  const int* cs_tgt, const double* sx, const double* sy, const double* sz,
+                  const double* sg, const int* cs_src, double* w) {
+  gauss_sum_impl(g, tx, ty, tz, cs_tgt, sx, sy, sz, sg, cs_src, w);
+  return OK;
+}
+
+int orc_buffer_counts(const orc_grid* g, const double* x, const double* y, const double* z,
+                      const int* cs, int* counts) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int ic = 0; ic < g->ncell; ic++) counts[ic] = buffer_set(g, ic, x, y, z, cs, nullptr);
+  return OK;
+}
+
+int orc_buffer_fill(const orc_grid* g, const double* x, const double* y, const double* z,
+                    const int* cs, const long long* offsets, int* idx) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int ic = 0; ic < g->ncell; ic++) buffer_set(g, ic, x, y, z, cs, idx + offsets[ic]);
+  return OK;
+}
+
+// Dense subdomain block, all pairs, no truncation (2d/matmult.cxx:83-93).
+int orc_block(const orc_grid* g, int nb, const int* idx, const double* x, const double* y,
+              const double* z, double* A) {
+  for (int i = 0; i < nb; i++)
+    for (int j = 0; j < nb; j++) {
+      int a = idx[i], b = idx[j];
+      double dz = g->dim == 3 ? z[a] - z[b] : 0.0;
+      A[(size_t)i * nb + j] = phi(g->sigma, x[a] - x[b], y[a] - y[b], dz, g->dim);
+    }
+  return OK;
+}
+
+void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y,
+                      const double* z, const int* cs, int* status) {
+  Rasm* R = new Rasm;
+  R->n = n;
+  R->ncell = g->ncell;
+  R->cs.assign(cs, cs + g->ncell + 1);
+  std::vector<int> cnt(g->ncell);
+  orc_buffer_counts(g, x, y, z, cs, cnt.data());
+  R->off.resize(g->ncell + 1);
+  R->aoff.resize(g->ncell + 1);
+  R->off[0] = 0;
+  R->aoff[0] = 0;
+  for (int c = 0; c < g->ncell; c++) {
+    R->off[c + 1] = R->off[c] + cnt[c];
+    R->aoff[c + 1] = R->aoff[c] + (long long)cnt[c] * cnt[c];
+  }
+  R->idx.resize(R->off[g->ncell]);
+  R->piv.resize(R->off[g->ncell]);
+  orc_buffer_fill(g, x, y, z, cs, R->off.data(), R->idx.data());
+  R->lu.resize(R->aoff[g->ncell]);
+  int bad = 0;
+  // mysubmat (2d/matmult.cxx:53-104) + the per-block dense LU of -sub_pc_type lu.
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+  for (int c = 0; c < g->ncell; c++) {
+    int nb = cnt[c];
+    if (!nb) continue;
+    double* A = R->lu.data() + R->aoff[c];
+    orc_block(g, nb, R->idx.data() + R->off[c], x, y, z, A);
+    if (lu_factor(nb, A, R->piv.data() + R->off[c])) bad = 1;
+  }
+  if (status) *status = bad ? ERR_SINGULAR : OK;
+  return R;
+}
+
+// Restricted additive Schwarz apply: subdomain = buffer set ("is"), prolongation only
+// onto the centre points ("is_local" = first n_c entries), 2d/rbf_interpolation.cxx:213-229.
+int orc_rasm_apply(void* h, const double* r, double* out) {
+  Rasm* R = (Rasm*)h;
+#pragma omp parallel
+  {
+    std::vector<double> buf;
+#pragma omp for schedule(dynamic, 4)
+    for (int c = 0; c < R->ncell; c++) {
+      long long nb = R->off[c + 1] - R->off[c];
+      if (!nb) continue;
+      buf.resize(nb);
+      const int* id = R->idx.data() + R->off[c];
+      for (long long i = 0; i < nb; i++) buf[i] = r[id[i]];
+      lu_solve((int)nb, R->lu.data() + R->aoff[c], R->piv.data() + R->off[c], buf.data());
+      int nc = R->cs[c + 1] - R->cs[c];
+      for (int i = 0; i < nc; i++) out[R->cs[c] + i] = buf[i];
+    }
+  }
+  return OK;
+}
+
+void orc_rasm_destroy(void* h) { delete (Rasm*)h; }
+
+// GMRES(restart), left preconditioning, classical Gram-Schmidt without refinement,
+// Givens rotations, preconditioned-residual convergence test relative to the first
+// preconditioned residual: PETSc KSPGMRES / KSPConvergedDefault defaults, invoked at
+// 2d/rbf_interpolation.cxx:210-232 with options 2d/Makefile:7. Restated from PETSc's
+// documented algorithm (PETSc is not part of the reference; parity unpinned).
+int orc_gmres(const orc_grid* g, int n, const double* x, const double* y, const double* z,
+              const int* cs, void* rasm, const double* b, const double* x0, double rtol,
+              double abstol, double dtol, int restart, int max_it, double* xsol, int* its_out,
+              int* reason_out, double* hist) {
+  const double haptol = 1e-30;
+  int m = restart;
+  std::vector<double> V((size_t)(m + 1) * n), t(n), w(n);
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cc(m), ss(m), grs(m + 1);
+  for (int i = 0; i < n; i++) xsol[i] = x0 ? x0[i] : 0.0;
+  auto apply_BA = [&](const double* v, double* out) {
+    gauss_sum_impl(g, x, y, z, cs, x, y, z, v, cs, t.data());
+    orc_rasm_apply(rasm, t.data(), out);
+  };
+  int its = 0, reason = 0;
+  double rnorm0 = 0, ttol = 0;
+  auto converged = [&](int k, double rnorm) -> int {
+    if (k == 0) {
+      rnorm0 = rnorm;
+      ttol = std::max(rtol * rnorm0, abstol);
+    }
+    if (rnorm != rnorm) return DIVERGED_NANORINF;
+    if (rnorm <= ttol) return rnorm < abstol ? CONVERGED_ATOL : CONVERGED_RTOL;
+    if (rnorm >= dtol * rnorm0) return DIVERGED_DTOL;
+    return 0;
+  };
+  while (!reason) {
+    // v0 = B (b - A x)
+    gauss_sum_impl(g, x, y, z, cs, x, y, z, xsol, cs, t.data());
+    for (int i = 0; i < n; i++) w[i] = b[i] - t[i];
+    double* v0 = V.data();
+    orc_rasm_apply(rasm, w.data(), v0);
+    double beta = sqrt(det_dot(n, v0, v0));
+    if (its == 0 && hist) hist[0] = beta;
+    if (beta == 0.0) {
+      reason = CONVERGED_ATOL;
+      break;
+    }
+    reason = converged(its, beta);
+    if (reason) break;
+    for (int i = 0; i < n; i++) v0[i] /= beta;
+    grs.assign(m + 1, 0.0);
+    grs[0] = beta;
+    int it = 0;
+    bool hapend = false;
+    while (!reason && it < m && its < max_it) {
+      double* vk = V.data() + (size_t)it * n;
+      double* vn = V.data() + (size_t)(it + 1) * n;
+      apply_BA(vk, vn);
+      // classical Gram-Schmidt: all coefficients from the same vector, then one update
+      std::vector<double> hcol(it + 2, 0.0);
+      for (int j = 0; j <= it; j++) hcol[j] = det_dot(n, vn, V.data() + (size_t)j * n);
+      for (int j = 0; j <= it; j++) {
+        const double* vj = V.data() + (size_t)j * n;
+        double hj = hcol[j];
+        for (int i = 0; i < n; i++) vn[i] -= hj * vj[i];
+      }
+      double tt = sqrt(det_dot(n, vn, vn));
+      double hapbnd = fabs(tt / grs[it]);
+      if (hapbnd > haptol) hapbnd = haptol;
+      if (tt > hapbnd) {
+        for (int i = 0; i < n; i++) vn[i] /= tt;
+      } else {
+        hapend = true;
+      }
+      hcol[it + 1] = tt;
+      // apply earlier rotations, build the new one, rotate the residual vector
+      for (int j = 0; j < it; j++) {
+        double a = hcol[j], bb = hcol[j + 1];
+        hcol[j] = cc[j] * a + ss[j] * bb;
+        hcol[j + 1] = -ss[j] * a + cc[j] * bb;
+      }
+      double rr = sqrt(hcol[it] * hcol[it] + hcol[it + 1] * hcol[it + 1]);
+      if (rr == 0.0) {
+        reason = DIVERGED_BREAKDOWN;
+        break;
+      }
+      cc[it] = hcol[it] / rr;
+      ss[it] = hcol[it + 1] / rr;
+      grs[it + 1] = -ss[it] * grs[it];
+      grs[it] = cc[it] * grs[it];
+      hcol[it] = cc[it] * hcol[it] + ss[it] * hcol[it + 1];
+      for (int j = 0; j <= it; j++) H[(size_t)j * m + it] = hcol[j];
+      double res = fabs(grs[it + 1]);
+      it++;
+      its++;
+      if (hist) hist[its] = res;
+      reason = converged(its, res);
+      if (hapend && !reason) reason = DIVERGED_BREAKDOWN;
+    }
+    // x += V y, H y = grs (upper triangular, size it)
+    if (it > 0) {
+      std::vector<double> yv(it);
+      for (int k = it - 1; k >= 0; k--) {
+        double s = grs[k];
+        for (int j = k + 1; j < it; j++) s -= H[(size_t)k * m + j] * yv[j];
+        double d = H[(size_t)k * m + k];
+        yv[k] = d != 0.0 ? s / d : 0.0;
+      }
+      for (int j = 0; j < it; j++) {
+        const double* vj = V.data() + (size_t)j * n;
+        for (int i = 0; i < n; i++) xsol[i] += yv[j] * vj[i];
+      }
+    }
+    if (!reason && its >= max_it) reason = DIVERGED_ITS;
+  }
+  if (its_out) *its_out = its;
+  if (reason_out) *reason_out = reason;
+  return OK;
+}
+
+// rbf_interpolation (2d/rbf_interpolation.cxx:25-310; 3d:26-334): bounding box, cell
+// sort, solve in cell order from a zero guess, weights back in the caller's order.
+int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, const double* z,
+                          const double* f, double sigma, int nsigma_box, int sigma_buffer,
+                          int sigma_trunc, double rtol, int restart, int max_it, double* g_out,
+                          int* its, int* reason) {
+  if (n <= 0) return ERR_ARG;
+  double b[6] = {x[0], x[0], y[0], y[0], dim == 3 ? z[0] : 0, dim == 3 ? z[0] : 0};
+  for (int i = 0; i < n; i++) {
+    b[0] = std::min(b[0], x[i]);
+    b[1] = std::max(b[1], x[i]);
+    b[2] = std::min(b[2], y[i]);
+    b[3] = std::max(b[3], y[i]);
+    if (dim == 3) {
+      b[4] = std::min(b[4], z[i]);
+      b[5] = std::max(b[5], z[i]);
+    }
+  }
+  orc_grid g;
+  int st = orc_grid_make(dim, b[0], b[1], b[2], b[3], b[4], b[5], sigma, nsigma_box,
+                         sigma_buffer, sigma_trunc, &g);
+  if (st) return st;
+  std::vector<int> perm(n), cs(g.ncell + 1);
+  st = orc_cell_sort(&g, n, x, y, z, perm.data(), cs.data());
+  if (st) return st;
+  std::vector<double> xs(n), ys(n), zs(dim == 3 ? n : 0), fs(n), gs(n);
+  for (int k = 0; k < n; k++) {
+    xs[k] = x[perm[k]];
+    ys[k] = y[perm[k]];
+    if (dim == 3) zs[k] = z[perm[k]];
+    fs[k] = f[perm[k]];
+  }
+  const double* zp = dim == 3 ? zs.data() : nullptr;
+  void* R = orc_rasm_create(&g, n, xs.data(), ys.data(), zp, cs.data(), &st);
+  if (st) {
+    orc_rasm_destroy(R);
+    return st;
+  }
+  orc_gmres(&g, n, xs.data(), ys.data(), zp, cs.data(), R, fs.data(), nullptr, rtol, 1e-50,
+            1e5, restart, max_it, gs.data(), its, reason, nullptr);
+  orc_rasm_destroy(R);
+  for (int k = 0; k < n; k++) g_out[perm[k]] = gs[k];
+  return OK;
+}
+
+// vorticity_evaluation (2d/vorticity_evaluation.cxx:26-299, 2d/get_vorticity.h:9-27):
+// one grid over the union bounding box, targets and sources each cell-sorted.
+int orc_vorticity_evaluation(int dim, int nt, const double* xt, const double* yt,
+                             const double* zt, int ns, const double* xs, const double* ys,
+                             const double* zs, const double* gs, double sigma, int nsigma_box,
+                             int sigma_buffer, int sigma_trunc, double* w_out) {
+  if (nt <= 0 || ns <= 0) return ERR_ARG;
+  double b[6] = {xt[0], xt[0], yt[0], yt[0], dim == 3 ? zt[0] : 0, dim == 3 ? zt[0] : 0};
+  auto upd = [&](int n, const double* x, const double* y, const double* z) {
+    for (int i = 0; i < n; i++) {
+      b[0] = std::min(b[0], x[i]);
+      b[1] = std::max(b[1], x[i]);
+      b[2] = std::min(b[2], y[i]);
+      b[3] = std::max(b[3], y[i]);
+      if (dim == 3) {
+        b[4] = std::min(b[4], z[i]);
+        b[5] = std::max(b[5], z[i]);
+      }
+    }
+  };
+  upd(nt, xt, yt, zt);
+  upd(ns, xs, ys, zs);
+  orc_grid g;
+  int st = orc_grid_make(dim, b[0], b[1], b[2], b[3], b[4], b[5], sigma, nsigma_box,
+                         sigma_buffer, sigma_trunc, &g);
+  if (st) return st;
+  std::vector<int> pt(nt), ps(ns), ct(g.ncell + 1), cs(g.ncell + 1);
+  if ((st = orc_cell_sort(&g, nt, xt, yt, zt, pt.data(), ct.data()))) return st;
+  if ((st = orc_cell_sort(&g, ns, xs, ys, zs, ps.data(), cs.data()))) return st;
+  std::vector<double> txs(nt), tys(nt), tzs(dim == 3 ? nt : 0), sxs(ns), sys(ns),
+      szs(dim == 3 ? ns : 0), sgs(ns), w(nt);
+  for (int k = 0; k < nt; k++) {
+    txs[k] = xt[pt[k]];
+    tys[k] = yt[pt[k]];
+    if (dim == 3) tzs[k] = zt[pt[k]];
+  }
+  for (int k = 0; k < ns; k++) {
+    sxs[k] = xs[ps[k]];
+    sys[k] = ys[ps[k]];
+    if (dim == 3) szs[k] = zs[ps[k]];
+    sgs[k] = gs[ps[k]];
+  }
+  gauss_sum_impl(&g, txs.data(), tys.data(), dim == 3 ? tzs.data() : nullptr, ct.data(),
+                 sxs.data(), sys.data(), dim == 3 ? szs.data() : nullptr, sgs.data(),
+                 cs.data(), w.data());
+  for (int k = 0; k < nt; k++) w_out[pt[k]] = w[k];
+  return OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+"""Seeded synthetic inputs and the error metric of the PetRBF drivers.
+
+The reference's drivers generate lattices and analytic fields in ``main``
+(2d/main.cxx:69-111, 3d/main.cxx) and report ``log10(||w-e||_2/||e||_2)``
+(2d/main.cxx:130-133). This module provides the same kind of inputs for the
+workloads this package is measured on, with numpy's PCG64 generator for the seeded
+jitter so the same seed gives the same points on every machine.
+
+Parameter mapping (widths are full box widths in units of sigma, as in the reference):
+cell edge 8 sigma -> nsigma_box = 8; cutoff 8 sigma past the cell edge ->
+sigma_trunc = 8 + 16 = 24 (the reference's "+16" rule, 2d/main2.cxx:64-65);
+one cell plus a one-cell overlap buffer -> sigma_buffer = 24.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+
+@dataclass
+class Problem:
+    name: str
+    x: np.ndarray
+    y: np.ndarray
+    z: object  # np.ndarray or None (2D)
+    f: np.ndarray  # right-hand side(s): (n,) or (n, nrhs)
+    sigma: float
+    nsigma_box: int
+    sigma_buffer: int
+    sigma_trunc: int
+    exact: object = None  # analytic field at the points (same shape as f)
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self):
+        return int(self.x.shape[0])
+
+    @property
+    def dim(self):
+        return 3 if self.z is not None else 2
+
+    def params(self):
+        return (self.sigma, self.nsigma_box, self.sigma_buffer, self.sigma_trunc)
+
+
+def lamb_oseen(x, y, G=1.0, nu=0.01, t=1.0, xc=0.0, yc=0.0):
+    """Lamb-Oseen vorticity G/(4 pi nu t) exp(-r^2/(4 nu t)) (2d/main.cxx:103, nu from
+    2d/main2.cxx:44)."""
+    r2 = (x - xc) ** 2 + (y - yc) ** 2
+    return G / (4.0 * math.pi * nu * t) * np.exp(-r2 / (4.0 * nu * t))
+
+
+def vortex_ring(x, y, z, R=0.5, a=0.1, gamma=1.0):
+    """Gaussian-core vortex ring about the z axis: |omega| = gamma/(pi a^2) exp(-s^2/a^2)
+    with s the distance to the core circle (rho = R, z = 0), directed along e_theta.
+    Returns (omega_x, omega_y, omega_z); omega_z is identically zero."""
+    rho = np.sqrt(x * x + y * y)
+    s2 = (rho - R) ** 2 + z * z
+    w = gamma / (math.pi * a * a) * np.exp(-s2 / (a * a))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ex = np.where(rho > 0, -y / np.where(rho > 0, rho, 1.0), 0.0)
+        ey = np.where(rho > 0, x / np.where(rho > 0, rho, 1.0), 0.0)
+    return w * ex, w * ey, np.zeros_like(w)
+
+
+def lattice_2d(m, lo=-1.0, hi=1.0, jitter=0.0, seed=12345):
+    """m x m lattice x_k = lo + k h, h = (hi-lo)/m, point i at (x[i//m], y[i%m]) like
+    2d/main.cxx:106-108; optional uniform jitter of +/- jitter*h per coordinate."""
+    h = (hi - lo) / m
+    k = np.arange(m, dtype=np.float64)
+    xs = lo + k * h
+    x = np.repeat(xs, m)
+    y = np.tile(xs, m)
+    if jitter:
+        rng = np.random.default_rng(seed)
+        x = x + rng.uniform(-jitter * h, jitter * h, x.shape[0])
+        y = y + rng.uniform(-jitter * h, jitter * h, y.shape[0])
+    return x, y, h
+
+
+def lattice_3d(m, lo=-1.0, hi=1.0, jitter=0.0, seed=12345):
+    h = (hi - lo) / m
+    k = lo + np.arange(m, dtype=np.float64) * h
+    X, Y, Z = np.meshgrid(k, k, k, indexing="ij")
+    x, y, z = X.ravel().copy(), Y.ravel().copy(), Z.ravel().copy()
+    if jitter:
+        rng = np.random.default_rng(seed)
+        x += rng.uniform(-jitter * h, jitter * h, x.shape[0])
+        y += rng.uniform(-jitter * h, jitter * h, y.shape[0])
+        z += rng.uniform(-jitter * h, jitter * h, z.shape[0])
+    return x, y, z, h
+
+
+def lamb_oseen_2d(m, jitter=0.0, seed=12345, overlap=0.8, nsigma_box=8, name=None):
+    """2D Lamb-Oseen interpolation on an m x m lattice over [-1,1]^2; sigma = h/overlap,
+    cell edge nsigma_box sigma, cutoff 8 sigma past the cell edge, one-cell buffer."""
+    x, y, h = lattice_2d(m, jitter=jitter, seed=seed)
+    e = lamb_oseen(x, y)
+    sigma = h / overlap
+    ntrunc = nsigma_box + 16
+    return Problem(name or "lamb_oseen_2d_%d" % m, x, y, None, e.copy(), sigma, nsigma_box,
+                   3 * nsigma_box, ntrunc, exact=e,
+                   meta={"m": m, "h": h, "jitter": jitter, "seed": seed, "overlap": overlap})
+
+
+def config1():
+    """2D plain FP64, N = 10^4 on a 100x100 lattice over [-1,1]^2 (h = 0.02)."""
+    return lamb_oseen_2d(100, name="2d_lamb_oseen_N1e4_lattice")
+
+
+def config2(m=2000, seed=12345):
+    """2D plain FP64 at scale: N = 4x10^6 on a 2000x2000 lattice, +/-0.25h seeded jitter."""
+    return lamb_oseen_2d(m, jitter=0.25, seed=seed, name="2d_lamb_oseen_N4e6_jitter")
+
+
+def config3(m=128, seed=12345, nsigma_box=2):
+    """3D vortex ring, N = 128^3 jittered lattice, three right-hand sides; cutoff 7 sigma
+    past the cell edge (sigma_trunc = nsigma_box + 14), one-cell buffer."""
+    x, y, z, h = lattice_3d(m, jitter=0.25, seed=seed)
+    wx, wy, wz = vortex_ring(x, y, z)
+    f = np.stack([wx, wy, wz], axis=1)
+    sigma = h / 0.8
+    return Problem("3d_vortex_ring_N%d" % (m ** 3), x, y, z, f.copy(), sigma, nsigma_box,
+                   3 * nsigma_box, nsigma_box + 14, exact=f,
+                   meta={"m": m, "h": h, "jitter": 0.25, "seed": seed})
+
+
+def log10_rel_error(w, e):
+    """log10(||w - e||_2 / ||e||_2), 2d/main.cxx:130-133."""
+    w = np.asarray(w, np.float64)
+    e = np.asarray(e, np.float64)
+    return float(np.log10(np.linalg.norm(w - e) / np.linalg.norm(e)))
