@@ -1,0 +1,142 @@
+/*
+ * petrbf_gb300.h -- C ABI of the GB300 implementation of PetRBF's solve path.
+ *
+ * Plain C types only (no CUDA or torch types). Every function returns an int status
+ * (PRBF_OK = 0) unless noted; no exception crosses this boundary. Host pointers unless
+ * the name ends in _dev. A context owns its device memory and one CUDA stream; use one
+ * context per host thread.
+ *
+ * Reference interfaces this ABI replaces (paths inside the petrbf project):
+ *   rbf_interpolation      2d/rbf_interpolation.cxx:25-26, 3d/rbf_interpolation.cxx:26-27
+ *   vorticity_evaluation   2d/vorticity_evaluation.cxx:26-27, 3d/vorticity_evaluation.cxx
+ *   MatShell MATOP_MULT    mymatmult, 2d/matmult.cxx:6 (registered at 2d/rbf_interpolation.cxx:190)
+ *   MATOP_GET_SUBMATRICES  mysubmat, 2d/matmult.cxx:53 (registered at 2d/rbf_interpolation.cxx:198)
+ *   RBFInterpolation       3d/wrapper.cxx:20-23 (library entry of librbf.a)
+ *   gpumatmult             2d/gpumatmult.cu:65-67 (the reference's C++ -> CUDA seam)
+ */
+#ifndef PETRBF_GB300_H
+#define PETRBF_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  PRBF_OK = 0,
+  PRBF_ERR_ARG = 1,           /* bad argument (null pointer, n <= 0, dim not 2/3, ...) */
+  PRBF_ERR_RANGE = 2,         /* parameters or coordinates outside the supported range */
+  PRBF_ERR_CAPACITY = 3,      /* a size exceeds a kernel or scratch capacity */
+  PRBF_ERR_CUDA = 4,          /* CUDA runtime error (message in prbf_last_error) */
+  PRBF_ERR_NOT_CONVERGED = 5, /* iteration limit reached (KSP_DIVERGED_ITS) */
+  PRBF_ERR_BREAKDOWN = 6,     /* GMRES breakdown (KSP_DIVERGED_BREAKDOWN) */
+  PRBF_ERR_NAN = 7,           /* NaN or Inf in the residual (KSP_DIVERGED_NANORINF) */
+  PRBF_ERR_STATE = 8,         /* call out of order (e.g. matvec before matvec_setup) */
+  PRBF_ERR_FACTOR = 9,        /* a subdomain block could not be factorised */
+  PRBF_ERR_DIVERGED = 10,     /* residual grew past dtol (KSP_DIVERGED_DTOL) */
+  PRBF_ERR_TIMEOUT = 11       /* a bounded device wait gave up (device error word set) */
+};
+
+/* Arithmetic of a solve. */
+enum {
+  PRBF_PREC_FP64 = 0,  /* FP64 matvec, FP64 block factors, FP64 GMRES (plain form) */
+  PRBF_PREC_MIXED = 1  /* FP32 matvec + FP32 block Cholesky inside FP64 iterative refinement */
+};
+
+/* Initial guess of a solve. */
+enum {
+  PRBF_GUESS_ZERO = 0,    /* zero initial guess, as the reference (no KSPSetInitialGuessNonzero) */
+  PRBF_GUESS_LEARNED = 1  /* per-cell MLP guess (requires prbf_guess_load) */
+};
+
+/* Flags of prbf_matvec_dev. */
+enum {
+  PRBF_ORDER_CALLER = 0, /* vectors in the order the points were given */
+  PRBF_ORDER_CELL = 1,   /* vectors in cell-sorted order (the solver's internal order) */
+  PRBF_MATVEC_FP32 = 2   /* FP32 pair arithmetic (the mixed-precision inner matvec) */
+};
+
+typedef struct {
+  int dim;           /* 2 or 3 */
+  double sigma;      /* Gaussian standard deviation */
+  int nsigma_box;    /* cell edge in units of sigma */
+  int sigma_buffer;  /* RASM subdomain box width in units of sigma */
+  int sigma_trunc;   /* truncation box width in units of sigma */
+  double rtol;       /* relative tolerance on the preconditioned residual (default 1e-13) */
+  double abstol;     /* absolute tolerance (default 1e-50) */
+  double dtol;       /* divergence tolerance (default 1e5) */
+  int restart;       /* GMRES restart length (default 30) */
+  int max_it;        /* iteration limit (default 1000) */
+  int precision;     /* PRBF_PREC_* */
+  int guess;         /* PRBF_GUESS_* */
+  int device;        /* CUDA device ordinal (default 0) */
+} prbf_params;
+
+typedef struct {
+  int its;                  /* Krylov iterations (KSPGetIterationNumber; inner total if mixed) */
+  int reason;               /* KSPConvergedReason-style code: 2 rtol, 3 atol, <0 diverged */
+  int outer_its;            /* iterative-refinement steps (mixed) */
+  int ncell;                /* cells of the grid */
+  int max_block;            /* largest RASM subdomain */
+  int nblocks_fallback;     /* blocks that needed a diagonal shift or FP64 refactor */
+  double rnorm0, rnorm;     /* first and last preconditioned residual norm */
+  double true_rel_resid;    /* ||f - A g||_2 / ||f||_2 in FP64 after the solve */
+  double t_sort_ms;         /* cell-list build */
+  double t_setup_ms;        /* RASM set-up (buffer lists, blocks, factors) */
+  double t_solve_ms;        /* Krylov / refinement iterations */
+  double t_total_ms;        /* whole call incl. host<->device copies */
+  long long pairs_per_matvec;
+} prbf_stats;
+
+typedef struct prbf_ctx prbf_ctx;
+
+void prbf_params_default(prbf_params* p);
+const char* prbf_status_string(int status);
+
+int prbf_ctx_create(const prbf_params* p, prbf_ctx** out);
+int prbf_ctx_destroy(prbf_ctx* ctx);
+/* Last error message of this context (valid until the next call on it). */
+const char* prbf_last_error(const prbf_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
+void* prbf_ctx_stream(prbf_ctx* ctx);
+int prbf_ctx_synchronize(prbf_ctx* ctx);
+
+/* rbf_interpolation: weights g with A g = f for n points; nrhs right-hand sides stored
+ * one after the other (f[r*n + i]); weights written the same way, in the caller's order.
+ * Replaces rbf_interpolation (2d/rbf_interpolation.cxx:25-26; 3d:26-27). z is ignored in
+ * 2D. */
+int prbf_interpolate(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z,
+                     const double* f, int nrhs, double* g_out, prbf_stats* stats);
+
+/* vorticity_evaluation: w_i = sum over the truncation set of g_j phi(|x_i - x_j|) at nt
+ * targets from ns sources (2d/vorticity_evaluation.cxx:26-27, 2d/get_vorticity.h:9-27). */
+int prbf_evaluate(prbf_ctx* ctx, int nt, const double* xt, const double* yt, const double* zt,
+                  int ns, const double* xs, const double* ys, const double* zs,
+                  const double* gs, double* w_out);
+
+/* MatShell seam: prbf_matvec_setup builds the cell list of n points on the GPU and keeps
+ * it resident; prbf_matvec then applies the truncated Gaussian operator like the
+ * reference's MATOP_MULT callback mymatmult (2d/matmult.cxx:6-51), host vectors in the
+ * caller's order. prbf_matvec_dev takes device pointers (PRBF_ORDER_* | PRBF_MATVEC_FP32). */
+int prbf_matvec_setup(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z);
+int prbf_matvec(prbf_ctx* ctx, const double* x_in, double* y_out);
+int prbf_matvec_dev(prbf_ctx* ctx, const double* x_in_dev, double* y_out_dev, int flags);
+/* Cell-list queries after prbf_matvec_setup: sorted position -> caller index, per-cell
+ * start offsets (ncell+1 ints), truncation-set sizes (ncell ints), and grid info
+ * (ints: nx ny nz ncell nb_trunc nb_buffer max_trunc; doubles: xmin ymin zmin box). */
+int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs);
+int prbf_get_permutation(prbf_ctx* ctx, int* perm_out);
+int prbf_get_cell_start(prbf_ctx* ctx, int* cell_start_out);
+int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
+
+/* RBFInterpolation (3d/wrapper.cxx:20-105): FP32 in/out, evaluates the particles
+ * (xp, yp, zp, gp) at the grid points first when xg[0] != xp[0], then solves on the
+ * grid and writes the weights over wg. argc/argv are accepted and ignored. */
+int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, float* zg,
+                          float* wg, int np, float* xp, float* yp, float* zp, float* gp,
+                          float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

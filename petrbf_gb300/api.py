@@ -1,0 +1,186 @@
+"""Python mirror of PetRBF's solve-path interface, running on the GPU through the C ABI.
+
+``rbf_interpolation`` and ``vorticity_evaluation`` keep the reference's argument
+meaning (2d/rbf_interpolation.cxx:25-26, 2d/vorticity_evaluation.cxx:26-27, and the 3d
+twins with z coordinates); ``GaussianOperator`` is the MatShell (MATOP_MULT =
+mymatmult, 2d/matmult.cxx:6-51). Errors raise ``PrbfError`` with the C status code.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from ._native import PrbfError, Stats
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+class Context:
+    """One GPU context (device memory + one CUDA stream) with fixed solver parameters."""
+
+    def __init__(self, dim=2, sigma=0.025, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
+                 rtol=1e-13, abstol=1e-50, dtol=1e5, restart=30, max_it=1000, precision="fp64",
+                 guess="zero", device=0):
+        L = N.lib()
+        p = N.Params()
+        L.prbf_params_default(ctypes.byref(p))
+        p.dim, p.sigma, p.nsigma_box = int(dim), float(sigma), int(nsigma_box)
+        p.sigma_buffer, p.sigma_trunc = int(sigma_buffer), int(sigma_trunc)
+        p.rtol, p.abstol, p.dtol = float(rtol), float(abstol), float(dtol)
+        p.restart, p.max_it, p.device = int(restart), int(max_it), int(device)
+        p.precision = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
+        p.guess = {"zero": N.GUESS_ZERO, "learned": N.GUESS_LEARNED}[guess]
+        self.params = p
+        self.dim = p.dim
+        h = ctypes.c_void_p()
+        st = L.prbf_ctx_create(ctypes.byref(p), ctypes.byref(h))
+        if st:
+            raise PrbfError(st, "prbf_ctx_create failed")
+        self.h = h
+        self.n = None
+
+    def _check(self, st):
+        if st:
+            raise PrbfError(st, N.lib().prbf_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().prbf_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return N.lib().prbf_ctx_stream(self.h)
+
+    def synchronize(self):
+        self._check(N.lib().prbf_ctx_synchronize(self.h))
+
+    # ---- MatShell seam -----------------------------------------------------------
+    def matvec_setup(self, x, y, z=None):
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        self.n = x.shape[0]
+        self._keep = (x, y, z)
+        self._check(N.lib().prbf_matvec_setup(self.h, self.n, _ptr(x), _ptr(y), _ptr(z)))
+
+    def matvec(self, v):
+        v = _f64(v)
+        out = np.empty_like(v)
+        self._check(N.lib().prbf_matvec(self.h, _ptr(v), _ptr(out)))
+        return out
+
+    def matvec_dev(self, in_ptr, out_ptr, cell_order=False, fp32=False):
+        flags = (N.ORDER_CELL if cell_order else 0) | (N.MATVEC_FP32 if fp32 else 0)
+        self._check(N.lib().prbf_matvec_dev(self.h, ctypes.c_void_p(in_ptr),
+                                             ctypes.c_void_p(out_ptr), flags))
+
+    def matvec_info(self):
+        ints = np.zeros(7, np.int32)
+        dbls = np.zeros(4, np.float64)
+        pairs = ctypes.c_longlong(0)
+        self._check(N.lib().prbf_matvec_info(self.h, ints.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                              _ptr(dbls), ctypes.byref(pairs)))
+        keys = ["nx", "ny", "nz", "ncell", "nb_trunc", "nb_buffer", "max_trunc"]
+        d = dict(zip(keys, (int(v) for v in ints)))
+        d.update(xmin=dbls[0], ymin=dbls[1], zmin=dbls[2], box=dbls[3], pairs=int(pairs.value))
+        return d
+
+    def permutation(self):
+        out = np.empty(self.n, np.int32)
+        self._check(N.lib().prbf_get_permutation(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out
+
+    def cell_start(self):
+        out = np.empty(self.matvec_info()["ncell"] + 1, np.int32)
+        self._check(N.lib().prbf_get_cell_start(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out
+
+    def trunc_counts(self):
+        out = np.empty(self.matvec_info()["ncell"], np.int32)
+        self._check(N.lib().prbf_get_trunc_counts(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out
+
+    # ---- solve and evaluation -------------------------------------------------------
+    def interpolate(self, x, y, z, f):
+        """Weights g with A g = f (f may hold several right-hand sides as columns)."""
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        f = np.asarray(f, np.float64)
+        n = x.shape[0]
+        nrhs = 1 if f.ndim == 1 else f.shape[1]
+        fr = np.ascontiguousarray(f.T if f.ndim == 2 else f)
+        g = np.empty_like(fr)
+        st = Stats()
+        self._check(N.lib().prbf_interpolate(self.h, n, _ptr(x), _ptr(y), _ptr(z), _ptr(fr), nrhs,
+                                              _ptr(g), ctypes.byref(st)))
+        return (g.T.copy() if f.ndim == 2 else g), st
+
+    def evaluate(self, xt, yt, zt, xs, ys, zs, gs):
+        xt, yt, zt, xs, ys, zs, gs = map(_f64, (xt, yt, zt, xs, ys, zs, gs))
+        w = np.empty(xt.shape[0], np.float64)
+        self._check(N.lib().prbf_evaluate(self.h, xt.shape[0], _ptr(xt), _ptr(yt), _ptr(zt), xs.shape[0],
+                                           _ptr(xs), _ptr(ys), _ptr(zs), _ptr(gs), _ptr(w)))
+        return w
+
+
+class GaussianOperator:
+    """The truncated Gaussian operator of a point set (the reference's MatShell M)."""
+
+    def __init__(self, x, y, z, sigma, nsigma_box, sigma_buffer, sigma_trunc, device=0):
+        self.ctx = Context(dim=3 if z is not None else 2, sigma=sigma, nsigma_box=nsigma_box,
+                           sigma_buffer=sigma_buffer, sigma_trunc=sigma_trunc, device=device)
+        self.ctx.matvec_setup(x, y, z)
+
+    def mult(self, v):
+        return self.ctx.matvec(v)
+
+    __matmul__ = mult
+
+
+def rbf_interpolation(xi, yi, *args, **opts):
+    """rbf_interpolation(xi, yi, [zi,] wi, sigma, nsigma_box, sigma_buffer, sigma_trunc)
+    -> (gi, its). Solves for the Gaussian weights gi that reproduce wi at the points
+    (2d/rbf_interpolation.cxx:25-26; 3d/rbf_interpolation.cxx:26-27)."""
+    if len(args) == 6:
+        zi, wi, sigma, nb, nbuf, nt = args
+    elif len(args) == 5:
+        zi = None
+        wi, sigma, nb, nbuf, nt = args
+    else:
+        raise TypeError("rbf_interpolation(xi, yi, [zi,] wi, sigma, nsigma_box, sigma_buffer, sigma_trunc)")
+    with Context(dim=3 if zi is not None else 2, sigma=sigma, nsigma_box=nb, sigma_buffer=nbuf,
+                 sigma_trunc=nt, **opts) as c:
+        g, st = c.interpolate(xi, yi, zi, wi)
+    return g, st.its
+
+
+def vorticity_evaluation(xi, yi, *args, **opts):
+    """vorticity_evaluation(xi, yi, [zi,] xj, yj, [zj,] gj, sigma, nsigma_box,
+    sigma_buffer, sigma_trunc) -> wi: the interpolant with weights gj at sources
+    (xj, yj[, zj]) evaluated at targets (xi, yi[, zi])
+    (2d/vorticity_evaluation.cxx:26-27, 2d/get_vorticity.h:9-27)."""
+    if len(args) == 9:
+        zi, xj, yj, zj, gj, sigma, nb, nbuf, nt = args
+    elif len(args) == 7:
+        zi = zj = None
+        xj, yj, gj, sigma, nb, nbuf, nt = args
+    else:
+        raise TypeError("vorticity_evaluation(xi, yi, [zi,] xj, yj, [zj,] gj, sigma, ...)")
+    with Context(dim=3 if zi is not None else 2, sigma=sigma, nsigma_box=nb, sigma_buffer=nbuf,
+                 sigma_trunc=nt, **opts) as c:
+        return c.evaluate(xi, yi, zi, xj, yj, zj, gj)

@@ -1,0 +1,101 @@
+// device.h -- device memory ownership and the kernel entry points shared between
+// translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace prbf {
+
+// Owning device buffer (cudaMalloc / cudaFree), grow-only.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  // Ensures capacity for `count` elements; contents are not preserved on growth.
+  T* reserve(size_t count) {
+    if (count <= n && p) return p;
+    release();
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    PRBF_CUDA(cudaMalloc((void**)&p, bytes));
+    n = count;
+    return p;
+  }
+  T* get() const { return p; }
+};
+
+// Temporary device storage handed to multi-kernel operations (sort, scans, Krylov
+// reductions). Slots are reused between calls and only ever grow.
+struct Workspace {
+  std::vector<DevBuf<unsigned char>*> slots;
+  ~Workspace() {
+    for (auto* s : slots) delete s;
+  }
+  void* get(int id, size_t bytes) {
+    while ((int)slots.size() <= id) slots.push_back(new DevBuf<unsigned char>());
+    return slots[id]->reserve(bytes < 256 ? 256 : bytes);
+  }
+};
+
+// ---- cellsort.cu -------------------------------------------------------------------
+// Min/max of each coordinate into out6 (device): xmin xmax ymin ymax zmin zmax.
+void bbox_dev(int n, const double* x, const double* y, const double* z, double* out6,
+              Workspace& ws, cudaStream_t s);
+// Exclusive scan of n values into out (in-place allowed); returns nothing, total is
+// out[n-1]+in[n-1] for callers that keep in.
+void scan_exclusive_dev(const int* in, int* out, long long n, Workspace& ws, int slot,
+                        cudaStream_t s);
+void scan_exclusive_dev(const long long* in, long long* out, long long n, Workspace& ws,
+                        int slot, cudaStream_t s);
+// Stable sort of n points into cells: perm[k] = caller index of the k-th sorted point,
+// cell_start[c] = first sorted position of cell c (ncell+1 entries). err receives
+// DEV_ERR_RANGE if a point lies outside the grid.
+void cell_sort_dev(const Grid& g, int n, const double* x, const double* y, const double* z,
+                   int* perm, int* cell_start, unsigned* err, Workspace& ws, cudaStream_t s);
+// out[k] = in[perm[k]] for k < n (double), and the inverse scatter out[perm[k]] = in[k].
+void gather_dev(int n, const int* perm, const double* in, double* out, cudaStream_t s);
+void scatter_dev(int n, const int* perm, const double* in, double* out, cudaStream_t s);
+
+// ---- gauss.cu ----------------------------------------------------------------------
+// Sorted point set on the device (SoA, padded so 16-byte bulk copies of any range stay
+// inside the allocation).
+struct PointsView {
+  int n;
+  const double* x;
+  const double* y;
+  const double* z;  // null in 2D
+  const int* cell_start;
+};
+
+// Work list of a truncated Gaussian sum: one item per (target cell, tile of targets).
+struct GaussPlan {
+  Grid g;
+  int nitems = 0;
+  int max_tile = 0;
+  long long pairs = 0;
+  int max_trunc = 0;
+  DevBuf<int2> items;     // (cell, first target of the tile)
+  DevBuf<int> trunc_cnt;  // truncation-set size per target cell
+};
+
+// Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc.
+void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src,
+                    unsigned* err, Workspace& ws, cudaStream_t s);
+// w[i] = sum_{j in trunc(cell(i))} g[j] exp(-|t_i - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
+// for all sorted targets i; g must be a padded device vector of src.n (+2) entries.
+void gauss_sum_dev(const GaussPlan& plan, const PointsView& tgt, const PointsView& src,
+                   const double* g, double* w, bool fp32, unsigned* err, cudaStream_t s);
+
+}  // namespace prbf

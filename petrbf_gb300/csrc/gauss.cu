@@ -1,0 +1,480 @@
+// gauss.cu -- truncated Gaussian sums on sm_103a: the matvec of the solve (mymatmult,
+// 2d/matmult.cxx:6-51; 3d/matmult.cxx:6-52) and the evaluation of the interpolant at
+// other targets (get_vorticity, 2d/get_vorticity.h:9-27).
+//
+//   w_i = sum_{j in T(c(i))} g_j exp(-|x_i - x_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
+//
+// T(c) is the truncation set of the target's cell c (2d/get_trunc.h:9-78): every source
+// of cell c, plus the sources of the cells within +-nb_trunc whose per-axis distance to
+// the centre of c is below trunc_len. The box test is evaluated in FP64 exactly as in the
+// reference, so the set is identical.
+//
+// One CTA works on one (target cell, tile of <= kTileT targets) item:
+//   1. the neighbour cells of a column (fixed jx [, jz], jy0..jy1) are one contiguous range
+//      of the cell-sorted source arrays; ranges are staged into shared memory with TMA bulk
+//      copies (cp.async.bulk) completing on an mbarrier (bounded wait);
+//   2. the CTA filters the staged sources with the box test and compacts the passing ones,
+//      in order, into a second shared buffer (as cell-relative, scaled coordinates);
+//   3. each warp takes groups of kGroup targets, its lanes stride over the compacted
+//      sources, and the partial sums are reduced with warp shuffles.
+// FP64 form: exp on the FP64 pipe with a table-folded polynomial (12 FP64 instructions
+// per pair, range reduction bits and the 2^-m scaling on the integer pipe). FP32 form:
+// FP32 coordinates relative to the cell centre and the SFU exp2.
+#include <algorithm>
+#include <cmath>
+
+#include "device.h"
+
+namespace prbf {
+namespace {
+
+constexpr int kThreads = 128;  // 4 warps
+constexpr int kWarps = kThreads / 32;
+constexpr int kTileT = 128;    // targets per work item
+constexpr int kGroup = 4;      // targets per warp pass
+constexpr int kRawCap = 1024;  // staged raw sources per fill (incl. alignment padding)
+constexpr int kMaxPieces = 64; // source ranges per fill
+
+// exp table: e^a with a = -L*d, d >= 0, L = ln2/kTab:  k = rint(d), r = k - d in [-1/2, 1/2],
+// e^a = 2^(-k/kTab) e^(L r) = 2^-m T[j] sum_i (L r)^i / i!,  k = m*kTab + j.
+constexpr int kTabBits = 8;
+constexpr int kTab = 1 << kTabBits;
+constexpr int kPoly = 5;  // degree-4 polynomial, coefficients T[j] L^i / i!
+__device__ double d_tab[kPoly][kTab];  // copied into shared memory by each CTA
+
+template <int DIM, bool F32>
+struct Cfg {
+  static constexpr int kComp = (F32 ? 2048 : (DIM == 3 ? 1536 : 2048));
+  using T = typename std::conditional<F32, float, double>::type;
+};
+
+struct Piece {
+  int raw_off;  // smem index of the first valid element
+  int count;    // valid elements
+  int gstart;   // global (sorted) index of the first valid element
+};
+
+constexpr size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// Dynamic shared memory carve-up of k_gauss (byte offsets, each 16-byte aligned).
+template <int DIM, bool F32>
+struct Layout {
+  using T = typename Cfg<DIM, F32>::T;
+  static constexpr int NA = DIM + 1;
+  static constexpr size_t raw = 0;
+  static constexpr size_t comp = align16(raw + sizeof(double) * NA * kRawCap);
+  static constexpr size_t tgt = align16(comp + sizeof(T) * NA * Cfg<DIM, F32>::kComp);
+  static constexpr size_t acc = align16(tgt + sizeof(T) * DIM * kTileT);
+  static constexpr size_t tab = align16(acc + sizeof(T) * kTileT);
+  static constexpr size_t pieces = align16(tab + (F32 ? 0 : sizeof(double) * kPoly * kTab));
+  static constexpr size_t bar = align16(pieces + sizeof(Piece) * kMaxPieces);
+  static constexpr size_t total = bar + 16;
+};
+
+__device__ __forceinline__ double hi_sub(double v, int m20) {
+  // v * 2^-m for a normal positive v: subtract m from the exponent field
+  int hi = __double2hiint(v) - m20;
+  return __hiloint2double(hi, __double2loint(v));
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+template <int DIM, bool F32>
+__global__ void __launch_bounds__(kThreads) k_gauss(
+    Grid g, const int2* __restrict__ items, const double* __restrict__ tx, const double* __restrict__ ty,
+    const double* __restrict__ tz, const int* __restrict__ cs_t, const double* __restrict__ sx,
+    const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
+    const int* __restrict__ cs_s, double* __restrict__ w, double scale, double norm, unsigned* err) {
+  using C = Cfg<DIM, F32>;
+  using T = typename C::T;
+  constexpr int NA = DIM + 1;  // staged arrays: coordinates + weight
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Layout<DIM, F32> lay;
+  double* raw = (double*)(smem + lay.raw);      // NA x kRawCap (FP64, as stored in HBM)
+  T* comp = (T*)(smem + lay.comp);              // NA x kComp (compacted truncation set)
+  T* tgt = (T*)(smem + lay.tgt);                // DIM x kTileT
+  T* acc = (T*)(smem + lay.acc);                // kTileT
+  double* tab = (double*)(smem + lay.tab);      // kPoly x kTab (FP64 form only)
+  Piece* pieces = (Piece*)(smem + lay.pieces);  // kMaxPieces
+  uint64_t* bar = (uint64_t*)(smem + lay.bar);
+  __shared__ int s_wsum[kWarps];
+  __shared__ int s_fill[3];  // npieces, valid total, done flag
+  __shared__ int s_cursor[2];
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int2 item = items[blockIdx.x];
+  const int ic = item.x, t0 = item.y;
+  const int nt = min(kTileT, cs_t[ic + 1] - t0);
+  int ix, iy, iz;
+  cell_xyz(g, ic, ix, iy, iz);
+  const double xc = centre_coord(g.xmin, ix, g.box);
+  const double yc = centre_coord(g.ymin, iy, g.box);
+  const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+  const double L = g.trunc_len;
+  const int c0 = cs_s[ic], c1 = cs_s[ic + 1];
+  const int nb = g.nb_trunc;
+  const int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+  const int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+  const int jz0 = DIM == 3 ? max(0, iz - nb) : 0, jz1 = DIM == 3 ? min(g.nz - 1, iz + nb) : 0;
+  const int ncolx = jx1 - jx0 + 1;
+  const int nranges = ncolx * (jz1 - jz0 + 1);
+
+  for (int t = tid; t < nt; t += kThreads) {
+    tgt[t] = (T)((tx[t0 + t] - xc) * scale);
+    tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
+    if (DIM == 3) tgt[2 * kTileT + t] = (T)((tz[t0 + t] - zc) * scale);
+    acc[t] = T(0);
+  }
+  if (!F32)
+    for (int i = tid; i < kPoly * kTab; i += kThreads) tab[i] = (&d_tab[0][0])[i];
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    s_cursor[0] = 0;  // range index
+    s_cursor[1] = -1; // position inside the range (-1: start of range)
+    s_abort = 0;
+  }
+  __syncthreads();
+
+  int ncomp = 0;
+  unsigned phase = 0;
+  const int ngroups = (nt + kGroup - 1) / kGroup;
+
+  // pair loop over comp[0, ncomp) for all targets of the tile
+  auto flush = [&]() {
+    for (int gi = wid; gi < ngroups; gi += kWarps) {
+      T tu[kGroup], tv[kGroup], tw[kGroup];
+      T a[kGroup];
+#pragma unroll
+      for (int k = 0; k < kGroup; k++) {
+        int t = min(gi * kGroup + k, nt - 1);
+        tu[k] = tgt[t];
+        tv[k] = tgt[kTileT + t];
+        tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : T(0);
+        a[k] = T(0);
+      }
+      for (int j = lane; j < ncomp; j += 32) {
+        T su = comp[j], sv = comp[C::kComp + j];
+        T sw = DIM == 3 ? comp[2 * C::kComp + j] : T(0);
+        T sgj = comp[(NA - 1) * C::kComp + j];
+#pragma unroll
+        for (int k = 0; k < kGroup; k++) {
+          T du = tu[k] - su, dv = tv[k] - sv;
+          T d2 = du * du;
+          d2 = fma(dv, dv, d2);
+          if (DIM == 3) {
+            T dw = tw[k] - sw;
+            d2 = fma(dw, dw, d2);
+          }
+          if constexpr (F32) {
+            a[k] = fmaf(sgj, ex2_approx(-d2), a[k]);
+          } else {
+            // d2 = |dx|^2 kTab / (2 sigma^2 ln2) >= 0;  k = rint(d2)
+            const double magic = 6755399441055744.0;  // 1.5 * 2^52
+            double kd = d2 + magic;
+            int kk = __double2loint(kd);
+            double r = (kd - magic) - d2;  // in [-1/2, 1/2]
+            int j8 = kk & (kTab - 1);
+            // m <= 900 keeps every scaled coefficient normal (2^-900 ~ 1e-271)
+            int m20 = min(kk >> kTabBits, 900) << 20;
+            double q = hi_sub(tab[4 * kTab + j8], m20);
+            q = fma(r, q, hi_sub(tab[3 * kTab + j8], m20));
+            q = fma(r, q, hi_sub(tab[2 * kTab + j8], m20));
+            q = fma(r, q, hi_sub(tab[1 * kTab + j8], m20));
+            q = fma(r, q, hi_sub(tab[j8], m20));
+            a[k] = fma(sgj, q, a[k]);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kGroup; k++) {
+        T s = warp_sum(a[k]);
+        int t = gi * kGroup + k;
+        if (lane == 0 && t < nt) acc[t] += s;
+      }
+    }
+    ncomp = 0;
+  };
+
+  while (true) {
+    // ---- plan and issue one fill (thread 0) -------------------------------------------
+    if (tid == 0) {
+      int r = s_cursor[0], p = s_cursor[1];
+      int used = 0, np = 0, valid = 0;
+      unsigned bytes = 0;
+      while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
+        int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+        int a = cs_s[cell_of(g, jx, jy0, jz)], b = cs_s[cell_of(g, jx, jy1, jz) + 1];
+        int s = p < 0 ? a : p;
+        if (s >= b) {
+          r++;
+          p = -1;
+          continue;
+        }
+        int s_al = s & ~1;
+        int room = (kRawCap - used) & ~1;
+        int e_al = min((b + 1) & ~1, s_al + room);
+        int e = min(b, e_al);
+        pieces[np].raw_off = used + (s - s_al);
+        pieces[np].count = e - s;
+        pieces[np].gstart = s;
+        np++;
+        valid += e - s;
+        used += e_al - s_al;
+        bytes += (unsigned)(e_al - s_al) * 8u * NA;
+        if (e >= b) {
+          r++;
+          p = -1;
+        } else {
+          p = e;
+        }
+      }
+      s_cursor[0] = r;
+      s_cursor[1] = p;
+      s_fill[0] = np;
+      s_fill[1] = valid;
+      s_fill[2] = (np == 0);
+      if (np > 0) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(bar, bytes);
+        for (int q = 0; q < np; q++) {
+          int s = pieces[q].gstart, s_al = s & ~1;
+          int len = ((s + pieces[q].count + 1) & ~1) - s_al;
+          int dst = pieces[q].raw_off - (s - s_al);
+          bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
+          bulk_g2s(raw + kRawCap + dst, sy + s_al, len * 8u, bar);
+          if (DIM == 3) bulk_g2s(raw + 2 * kRawCap + dst, sz + s_al, len * 8u, bar);
+          bulk_g2s(raw + (NA - 1) * kRawCap + dst, sg + s_al, len * 8u, bar);
+        }
+      }
+    }
+    __syncthreads();
+    if (s_fill[2]) break;
+    if (!mbar_wait(bar, phase)) {
+      if (tid == 0) {
+        atomicOr(err, DEV_ERR_TIMEOUT);
+        s_abort = 1;
+      }
+    }
+    phase ^= 1u;
+    __syncthreads();
+    if (s_abort) {
+      // let the copies of this fill land (bounded) before the CTA exits
+      mbar_wait(bar, phase ^ 1u, 1u << 20);
+      return;
+    }
+    // ---- make room, then filter + compact in order ----------------------------------
+    if (ncomp + s_fill[1] > C::kComp) {
+      flush();
+      __syncthreads();
+    }
+    const int np = s_fill[0];
+    for (int q = 0; q < np; q++) {
+      const Piece pc = pieces[q];
+      for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
+        int e = e0 + tid;
+        bool in = false;
+        double vx = 0, vy = 0, vz = 0, vg = 0;
+        if (e < pc.count) {
+          int j = pc.gstart + e, ro = pc.raw_off + e;
+          vx = raw[ro];
+          vy = raw[kRawCap + ro];
+          if (DIM == 3) vz = raw[2 * kRawCap + ro];
+          vg = raw[(NA - 1) * kRawCap + ro];
+          // centre cell unconditionally (2d/get_trunc.h:31-39), neighbours by the box test
+          // fabs(xj - xc) < trunc_length && ... (2d/get_trunc.h:63; 3d/get_trunc.h:70-72)
+          bool boxin = fabs(vx - xc) < L && fabs(vy - yc) < L;
+          if (DIM == 3) boxin = boxin && fabs(vz - zc) < L;
+          in = (j >= c0 && j < c1) || boxin;
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, in);
+        if (lane == 0) s_wsum[wid] = __popc(bal);
+        __syncthreads();
+        int pre = 0, tot = 0;
+#pragma unroll
+        for (int k = 0; k < kWarps; k++) {
+          int c = s_wsum[k];
+          pre += k < wid ? c : 0;
+          tot += c;
+        }
+        if (in) {
+          int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
+          comp[pos] = (T)((vx - xc) * scale);
+          comp[C::kComp + pos] = (T)((vy - yc) * scale);
+          if (DIM == 3) comp[2 * C::kComp + pos] = (T)((vz - zc) * scale);
+          comp[(NA - 1) * C::kComp + pos] = (T)vg;
+        }
+        ncomp += tot;
+        __syncthreads();
+      }
+    }
+  }
+  flush();
+  __syncthreads();
+  for (int t = tid; t < nt; t += kThreads) w[t0 + t] = (double)acc[t] * norm;
+}
+
+// ---- work list and truncation-set sizes ----------------------------------------------
+__global__ void k_item_counts(int ncell, const int* __restrict__ cs_t, int* __restrict__ cnt) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncell) cnt[c] = (cs_t[c + 1] - cs_t[c] + kTileT - 1) / kTileT;
+}
+
+__global__ void k_item_fill(int ncell, const int* __restrict__ cs_t, const int* __restrict__ off,
+                            int2* __restrict__ items) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  int a = cs_t[c], b = cs_t[c + 1], o = off[c];
+  for (int t = a; t < b; t += kTileT) items[o++] = make_int2(c, t);
+}
+
+// One warp per target cell: size of its truncation set (0 for an empty target cell,
+// 2d/get_trunc.h:76-78); accumulates the pair count and the maximum.
+__global__ void k_trunc_count(Grid g, const int* __restrict__ cs_t, const double* __restrict__ sx,
+                              const double* __restrict__ sy, const double* __restrict__ sz,
+                              const int* __restrict__ cs_s, int* __restrict__ cnt,
+                              unsigned long long* __restrict__ pairs, int* __restrict__ maxc) {
+  int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (c >= g.ncell) return;
+  int ntg = cs_t[c + 1] - cs_t[c];
+  if (ntg == 0) {
+    if (lane == 0) cnt[c] = 0;
+    return;
+  }
+  int ix, iy, iz;
+  cell_xyz(g, c, ix, iy, iz);
+  double xc = centre_coord(g.xmin, ix, g.box), yc = centre_coord(g.ymin, iy, g.box);
+  double zc = g.dim == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+  double L = g.trunc_len;
+  int nb = g.nb_trunc;
+  int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+  int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+  int jz0 = g.dim == 3 ? max(0, iz - nb) : 0, jz1 = g.dim == 3 ? min(g.nz - 1, iz + nb) : 0;
+  int c0 = cs_s[c], c1 = cs_s[c + 1];
+  int n = 0;
+  for (int jz = jz0; jz <= jz1; jz++)
+    for (int jx = jx0; jx <= jx1; jx++) {
+      int a = cs_s[cell_of(g, jx, jy0, jz)], b = cs_s[cell_of(g, jx, jy1, jz) + 1];
+      for (int j = a + lane; j < b; j += 32) {
+        bool in = fabs(sx[j] - xc) < L && fabs(sy[j] - yc) < L;
+        if (g.dim == 3) in = in && fabs(sz[j] - zc) < L;
+        n += ((j >= c0 && j < c1) || in) ? 1 : 0;
+      }
+    }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if (lane == 0) {
+    cnt[c] = n;
+    atomicAdd(pairs, (unsigned long long)n * (unsigned long long)ntg);
+    atomicMax(maxc, n);
+  }
+}
+
+bool g_tab_ready[64] = {false};
+
+void upload_table(cudaStream_t s) {
+  int dev = 0;
+  PRBF_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && g_tab_ready[dev]) return;
+  // T[j] = 2^(-j/kTab) in long double, then the folded Taylor coefficients T L^i / i!
+  static double h[kPoly][kTab];
+  const long double L = logl(2.0L) / kTab;
+  for (int j = 0; j < kTab; j++) {
+    long double t = exp2l(-(long double)j / kTab);
+    long double f = 1.0L, lp = 1.0L;
+    for (int i = 0; i < kPoly; i++) {
+      h[i][j] = (double)(t * lp / f);
+      lp *= L;
+      f *= (long double)(i + 1);
+    }
+  }
+  PRBF_CUDA(cudaMemcpyToSymbolAsync(d_tab, h, sizeof(h), 0, cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  if (dev < 64) g_tab_ready[dev] = true;
+}
+
+template <int DIM, bool F32>
+size_t smem_bytes() {
+  return Layout<DIM, F32>::total;
+}
+
+template <int DIM, bool F32>
+void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
+            unsigned* err, cudaStream_t st) {
+  size_t sm = smem_bytes<DIM, F32>();
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  PRBF_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !attr_set[dev]) {
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss<DIM, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (dev < 64) attr_set[dev] = true;
+  }
+  const double sigma = P.g.sigma;
+  const double norm = 1.0 / (2 * M_PI * sigma * sigma);
+  // FP64: squared scaled distance in units of ln2/kTab;  FP32: in units of ln2 (exp2)
+  const double scale = F32 ? std::sqrt(1.0 / (2.0 * sigma * sigma * std::log(2.0)))
+                           : std::sqrt((double)kTab / (2.0 * sigma * sigma * std::log(2.0)));
+  k_gauss<DIM, F32><<<P.nitems, kThreads, sm, st>>>(P.g, P.items.get(), t.x, t.y, t.z, t.cell_start,
+                                                    s.x, s.y, s.z, gv, s.cell_start, w, scale, norm, err);
+  PRBF_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src, unsigned* err,
+                    Workspace& ws, cudaStream_t s) {
+  (void)err;
+  const Grid& g = plan.g;
+  int* cnt = (int*)ws.get(20, sizeof(int) * ((size_t)g.ncell + 1));
+  k_item_counts<<<ceil_div(g.ncell, 256), 256, 0, s>>>(g.ncell, tgt.cell_start, cnt);
+  PRBF_CHECK_LAUNCH();
+  PRBF_CUDA(cudaMemsetAsync(cnt + g.ncell, 0, sizeof(int), s));
+  scan_exclusive_dev(cnt, cnt, (long long)g.ncell + 1, ws, 21, s);
+  int nitems = 0;
+  PRBF_CUDA(cudaMemcpyAsync(&nitems, cnt + g.ncell, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  plan.nitems = nitems;
+  plan.items.reserve(std::max(nitems, 1));
+  k_item_fill<<<ceil_div(g.ncell, 256), 256, 0, s>>>(g.ncell, tgt.cell_start, cnt, plan.items.get());
+  PRBF_CHECK_LAUNCH();
+  plan.trunc_cnt.reserve(g.ncell);
+  struct {
+    unsigned long long pairs;
+    int maxc;
+    int pad;
+  } h{0, 0, 0};
+  void* d = ws.get(24, sizeof(h));
+  PRBF_CUDA(cudaMemsetAsync(d, 0, sizeof(h), s));
+  k_trunc_count<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, tgt.cell_start, src.x, src.y, src.z,
+                                                     src.cell_start, plan.trunc_cnt.get(),
+                                                     (unsigned long long*)d, (int*)((char*)d + 8));
+  PRBF_CHECK_LAUNCH();
+  PRBF_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  plan.pairs = (long long)h.pairs;
+  plan.max_trunc = h.maxc;
+  plan.max_tile = kTileT;
+  upload_table(s);
+}
+
+void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv,
+                   double* w, bool fp32, unsigned* err, cudaStream_t st) {
+  if (P.nitems == 0) return;
+  if (P.g.dim == 2) {
+    if (fp32)
+      launch<2, true>(P, t, s, gv, w, err, st);
+    else
+      launch<2, false>(P, t, s, gv, w, err, st);
+  } else {
+    if (fp32)
+      launch<3, true>(P, t, s, gv, w, err, st);
+    else
+      launch<3, false>(P, t, s, gv, w, err, st);
+  }
+}
+
+}  // namespace prbf
