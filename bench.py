@@ -1,0 +1,358 @@
+"""Benchmark of the GB300 PetRBF solve path.
+
+Workload: the 2D Lamb-Oseen interpolation at scale -- N = 4x10^6 points on a 2000 x 2000
+lattice over [-1,1]^2 with seeded +/-0.25h jitter, sigma = h/0.8, cell edge 8 sigma,
+cutoff 8 sigma past the cell edge (sigma_trunc 24), one-cell overlap buffer (24).
+
+A step is one truncated Gaussian matvec (the operator GMRES applies every iteration,
+mymatmult of 2d/matmult.cxx:6-51) over all 4x10^6 points in FP64; ``value`` is
+Gpairs/s with the points resident in HBM and L2 flushed between steps; ``e2e`` is the
+same metric through the C ABI (prbf_matvec) with pinned host vectors copied in and out
+every step. The full solve to 1e-13 (plain FP64 and mixed precision) is timed once
+after the steps and reported under ``solve``.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--skip-solve]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_PAIR = 15  # the reference's count per pair, exp counted as 1 (2d/matmult.cxx:44-45)
+CPU_SAMPLE_M = 1000  # CPU baseline sample: 1000 x 1000 jittered lattice, same geometry
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-solve", action="store_true")
+    ap.add_argument("--m", type=int, default=2000, help="lattice edge (N = m^2)")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as td
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        td.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def allmax(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev, self.rows, self.stop = dev, [], False
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop:
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([c.strip() for c in out.split(",")])
+            except Exception:
+                pass
+            time.sleep(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 2 + k and r[2 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def fp64_peak_tflops(torch):
+    """FP64 peak measured in-run: cuBLAS DGEMM 8192^3 (2 N^3 flops), best of 5."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def profile_traffic(name):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(seconds_target=10.0):
+    """The oracle (C++ restatement of mymatmult, OpenMP over cells) on a bounded sample:
+    a 1000 x 1000 jittered lattice with the workload's geometry (same pairs per point)."""
+    import oracle as O
+    from petrbf_gb300 import workloads as W
+    p = W.lamb_oseen_2d(CPU_SAMPLE_M, jitter=0.25, seed=12345)
+    g = O.grid_for(p.x, p.y, None, *p.params())
+    perm, cs = O.cell_sort(g, p.x, p.y)
+    xs, ys = p.x[perm], p.y[perm]
+    pairs = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
+    v = np.random.default_rng(1).standard_normal(p.n)
+    O.matvec(g, xs, ys, None, cs, v)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.matvec(g, xs, ys, None, cs, v)
+        reps += 1
+        if time.perf_counter() - t0 >= seconds_target or reps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": pairs * reps / dt / 1e9, "unit": "Gpairs/s", "cores": O.num_threads(),
+            "kind": "port",
+            "sample": "%d FP64 matvecs of a %dx%d jittered lattice (%.3g pairs each), %.1f s" % (
+                reps, CPU_SAMPLE_M, CPU_SAMPLE_M, pairs, dt)}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU matvec (the oracle port; the reference's
+    compiled sources are not available on this machine) on all host cores."""
+    if rank != 0:
+        return
+    import oracle as O
+    from petrbf_gb300 import workloads as W
+    p = W.lamb_oseen_2d(CPU_SAMPLE_M, jitter=0.25, seed=12345)
+    g = O.grid_for(p.x, p.y, None, *p.params())
+    perm, cs = O.cell_sort(g, p.x, p.y)
+    xs, ys = p.x[perm], p.y[perm]
+    pairs = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
+    v = np.random.default_rng(1).standard_normal(p.n)
+    for _ in range(args.warmup):
+        O.matvec(g, xs, ys, None, cs, v)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.matvec(g, xs, ys, None, cs, v)
+    dt = time.perf_counter() - t0
+    val = pairs * args.steps / dt / 1e9
+    sample = "%d FP64 matvecs of a %dx%d jittered lattice (%.3g pairs each)" % (
+        args.steps, CPU_SAMPLE_M, CPU_SAMPLE_M, pairs)
+    print(json.dumps({
+        "impl": "reference", "metric": "Gaussian matvec Gpairs/s", "value": val, "unit": "Gpairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "2d_lamb_oseen_N4e6_jitter matvec (CPU sample N=1e6, same geometry)",
+                   "sigma_over_h": 1.25, "nsigma_box": 8, "sigma_buffer": 24, "sigma_trunc": 24},
+        "cpu_baseline": {"value": val, "unit": "Gpairs/s", "cores": O.num_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": val, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def offgrid_error(ctx, p, g, torch_rng_seed=7, nt=1_000_000):
+    """log10 relative error of the interpolant against the analytic field at nt random
+    targets inside the lattice (off the collocation points), 2d/main.cxx:130-133."""
+    from petrbf_gb300 import workloads as W
+    rng = np.random.default_rng(torch_rng_seed)
+    lo, hi = float(p.x.min()), float(p.x.max())
+    xt, yt = rng.uniform(lo, hi, nt), rng.uniform(lo, hi, nt)
+    w = ctx.evaluate(xt, yt, None, p.x, p.y, None, g)
+    return W.log10_rel_error(w, W.lamb_oseen(xt, yt))
+
+
+def run_ours(args, rank, world):
+    import torch
+    from petrbf_gb300 import workloads as W
+    from petrbf_gb300.api import Context
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    p = W.lamb_oseen_2d(args.m, jitter=0.25, seed=12345 + rank)
+    ctx = Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24, device=dev)
+    ctx.matvec_setup(p.x, p.y)
+    info = ctx.matvec_info()
+    pairs = info["pairs"]
+    n = p.n
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    vin = torch.randn(n, dtype=torch.float64, device="cuda")
+    vout = torch.empty_like(vin)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        ctx.matvec_dev(vin.data_ptr(), vout.data_ptr(), cell_order=True)
+    ctx.synchronize()
+    # ---- device-resident steps ------------------------------------------------------------
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    with Clocks(dev) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t_wall0 = time.perf_counter()
+        for e0, e1 in evs:
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0.record(stream)
+            ctx.matvec_dev(vin.data_ptr(), vout.data_ptr(), cell_order=True)
+            e1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        barrier(world)
+        t_wall = time.perf_counter() - t_wall0
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    ms = allmax(ms, world)
+    value = pairs * args.steps * world / (ms * 1e-3) / 1e9
+    # ---- end to end through the C ABI with pinned host vectors ----------------------------------
+    hin = torch.randn(n, dtype=torch.float64).pin_memory()
+    hout = torch.empty(n, dtype=torch.float64).pin_memory()
+    import ctypes
+    from petrbf_gb300 import _native as N
+    L = N.lib()
+    pin = ctypes.cast(hin.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    pout = ctypes.cast(hout.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    for _ in range(max(1, args.warmup)):
+        assert L.prbf_matvec(ctx.h, pin, pout) == 0
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert L.prbf_matvec(ctx.h, pin, pout) == 0
+    e2e_s = allmax(time.perf_counter() - t0, world)
+    e2e = pairs * args.steps * world / e2e_s / 1e9
+    # FP32 pair arithmetic of the same operator (the mixed form's inner matvec)
+    for _ in range(3):
+        ctx.matvec_dev(vin.data_ptr(), vout.data_ptr(), cell_order=True, fp32=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(20):
+        ctx.matvec_dev(vin.data_ptr(), vout.data_ptr(), cell_order=True, fp32=True)
+    e1.record(stream)
+    e1.synchronize()
+    fp32_gpairs = pairs * 20 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    ctx.close()
+    del flush, vin, vout
+    torch.cuda.empty_cache()
+
+    peak = fp64_peak_tflops(torch) if rank == 0 else None
+    achieved = FLOPS_PER_PAIR * pairs / (ms / args.steps * 1e-3) / 1e12
+    result = {
+        "metric": "Gaussian matvec Gpairs/s", "value": value, "unit": "Gpairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "2d_lamb_oseen_N4e6_jitter" if args.m == 2000 else "2d_lamb_oseen_m%d" % args.m,
+                   "n_points": n, "sigma_over_h": 1.25, "nsigma_box": 8, "sigma_buffer": 24,
+                   "sigma_trunc": 24, "pairs_per_matvec": pairs, "ncell": info["ncell"],
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None,
+                     "peak_source": "in-run cuBLAS DGEMM 8192^3 (no FP64 figure in MEASURED_PEAKS)",
+                     "flops_per_pair": FLOPS_PER_PAIR,
+                     "traffic": profile_traffic("gauss_fp64_2d_N4e6.txt")},
+        "fp32_matvec_gpairs": fp32_gpairs,
+        "wall_s_timed_region": t_wall,
+    }
+    if rank == 0 and world == 1:
+        result["cpu_baseline"] = cpu_baseline()
+    if not args.skip_solve:
+        result["solve"] = solve_section(p, dev, rank)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def solve_section(p, dev, rank):
+    """Time-to-1e-13 of the full interpolation (cell list, RASM set-up, Krylov), plain FP64
+    (the reference's algorithm) and mixed precision, with the off-grid interpolation error."""
+    from petrbf_gb300.api import Context
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
+                     precision=prec, device=dev) as c:
+            t0 = time.perf_counter()
+            g, st = c.interpolate(p.x, p.y, None, p.f)
+            wall = time.perf_counter() - t0
+            err = offgrid_error(c, p, g)
+        dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
+        out[prec] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s,
+                     "its": st.its, "outer_its": st.outer_its, "reason": st.reason,
+                     "true_rel_resid": st.true_rel_resid, "log10_err_offgrid": err,
+                     "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms,
+                     "t_solve_ms": st.t_solve_ms, "max_block": st.max_block,
+                     "blocks_shifted": st.nblocks_fallback}
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed"]["time_s"]
+    out["metric"] = "pts/s to 1e-13 residual"
+    return out
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

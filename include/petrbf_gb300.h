@@ -129,6 +129,14 @@ int prbf_get_permutation(prbf_ctx* ctx, int* perm_out);
 int prbf_get_cell_start(prbf_ctx* ctx, int* cell_start_out);
 int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
 
+/* RASM preconditioner of the points given to prbf_matvec_setup: the reference's P shell
+ * (MATOP_GET_SUBMATRICES = mysubmat, 2d/matmult.cxx:53-104) applied as PCASM with the
+ * restricted prolongation of 2d/rbf_interpolation.cxx:213-229. precision PRBF_PREC_FP64
+ * factorises the blocks in FP64, PRBF_PREC_MIXED in FP32. prbf_pc_apply computes z = B r
+ * (host vectors, caller order). */
+int prbf_pc_setup(prbf_ctx* ctx, int precision);
+int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
+
 /* RBFInterpolation (3d/wrapper.cxx:20-105): FP32 in/out, evaluates the particles
  * (xp, yp, zp, gp) at the grid points first when xg[0] != xp[0], then solves on the
  * grid and writes the weights over wg. argc/argv are accepted and ignored. */

@@ -116,6 +116,15 @@ class Context:
         self._check(N.lib().prbf_get_trunc_counts(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return out
 
+    def pc_setup(self, precision="fp64"):
+        self._check(N.lib().prbf_pc_setup(self.h, {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]))
+
+    def pc_apply(self, r):
+        r = _f64(r)
+        out = np.empty_like(r)
+        self._check(N.lib().prbf_pc_apply(self.h, _ptr(r), _ptr(out)))
+        return out
+
     # ---- solve and evaluation -------------------------------------------------------
     def interpolate(self, x, y, z, f):
         """Weights g with A g = f (f may hold several right-hand sides as columns)."""
@@ -167,6 +176,22 @@ def rbf_interpolation(xi, yi, *args, **opts):
                  sigma_trunc=nt, **opts) as c:
         g, st = c.interpolate(xi, yi, zi, wi)
     return g, st.its
+
+
+def RBFInterpolation(xg, yg, zg, wg, xp, yp, zp, gp, sigma, nsigma_box, sigma_buffer,
+                     sigma_trunc):
+    """The librbf.a entry (3d/wrapper.cxx:20-105): FP32 arrays; evaluates the particles
+    (xp, yp, zp, gp) at the grid first when xg[0] != xp[0], solves on the grid and
+    writes the weights over wg (in place). Returns the status code."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (xg, yg, zg, xp, yp, zp, gp)]
+    if not (isinstance(wg, np.ndarray) and wg.dtype == np.float32 and wg.flags.c_contiguous):
+        raise TypeError("wg must be a contiguous float32 array (it is overwritten)")
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    xg_, yg_, zg_, xp_, yp_, zp_, gp_ = arrs
+    return N.lib().prbf_RBFInterpolation(0, None, len(xg_), fp(xg_), fp(yg_), fp(zg_), fp(wg),
+                                         len(xp_), fp(xp_), fp(yp_), fp(zp_), fp(gp_),
+                                         float(sigma), int(nsigma_box), int(sigma_buffer),
+                                         int(sigma_trunc))
 
 
 def vorticity_evaluation(xi, yi, *args, **opts):

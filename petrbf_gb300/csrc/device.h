@@ -96,6 +96,7 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
 // w[i] = sum_{j in trunc(cell(i))} g[j] exp(-|t_i - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
 // for all sorted targets i; g must be a padded device vector of src.n (+2) entries.
 void gauss_sum_dev(const GaussPlan& plan, const PointsView& tgt, const PointsView& src,
-                   const double* g, double* w, bool fp32, unsigned* err, cudaStream_t s);
+                   const double* g, double* w, bool fp32, unsigned* err, cudaStream_t s,
+                   const int* skip = nullptr);
 
 }  // namespace prbf

@@ -18,8 +18,9 @@
 //   3. each warp takes groups of kGroup targets, its lanes stride over the compacted
 //      sources, and the partial sums are reduced with warp shuffles.
 // FP64 form: exp on the FP64 pipe with a table-folded polynomial (12 FP64 instructions
-// per pair, range reduction bits and the 2^-m scaling on the integer pipe). FP32 form:
-// FP32 coordinates relative to the cell centre and the SFU exp2.
+// per pair, range reduction bits and the 2^-m scaling on the integer pipe); coordinates
+// relative to the cell centre, unscaled, so x_t - x_s rounds as in the reference. FP32
+// form: scaled FP32 coordinates relative to the cell centre and the SFU exp2.
 #include <algorithm>
 #include <cmath>
 
@@ -88,7 +89,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
     Grid g, const int2* __restrict__ items, const double* __restrict__ tx, const double* __restrict__ ty,
     const double* __restrict__ tz, const int* __restrict__ cs_t, const double* __restrict__ sx,
     const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
-    const int* __restrict__ cs_s, double* __restrict__ w, double scale, double norm, unsigned* err) {
+    const int* __restrict__ cs_s, double* __restrict__ w, double scale, double kexp, double norm,
+    unsigned* err, const int* __restrict__ skip) {
+  if (skip && *skip) return;
   using C = Cfg<DIM, F32>;
   using T = typename C::T;
   constexpr int NA = DIM + 1;  // staged arrays: coordinates + weight
@@ -173,11 +176,13 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
           if constexpr (F32) {
             a[k] = fmaf(sgj, ex2_approx(-d2), a[k]);
           } else {
-            // d2 = |dx|^2 kTab / (2 sigma^2 ln2) >= 0;  k = rint(d2)
+            // d2 = |x_t - x_s|^2 (unscaled: the differences are exact as in the reference);
+            // in units of L = ln2/kTab the exponent is kexp*d2, kexp = kTab/(2 sigma^2 ln2):
+            // k = rint(kexp d2) (fused), r = k - kexp d2 in [-1/2, 1/2] with a single rounding
             const double magic = 6755399441055744.0;  // 1.5 * 2^52
-            double kd = d2 + magic;
+            double kd = fma(d2, kexp, magic);
             int kk = __double2loint(kd);
-            double r = (kd - magic) - d2;  // in [-1/2, 1/2]
+            double r = fma(-d2, kexp, kd - magic);
             int j8 = kk & (kTab - 1);
             // m <= 900 keeps every scaled coefficient normal (2^-900 ~ 1e-271)
             int m20 = min(kk >> kTabBits, 900) << 20;
@@ -404,7 +409,7 @@ size_t smem_bytes() {
 
 template <int DIM, bool F32>
 void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
-            unsigned* err, cudaStream_t st) {
+            unsigned* err, const int* skip, cudaStream_t st) {
   size_t sm = smem_bytes<DIM, F32>();
   static bool attr_set[64] = {false};
   int dev = 0;
@@ -415,11 +420,13 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   }
   const double sigma = P.g.sigma;
   const double norm = 1.0 / (2 * M_PI * sigma * sigma);
-  // FP64: squared scaled distance in units of ln2/kTab;  FP32: in units of ln2 (exp2)
-  const double scale = F32 ? std::sqrt(1.0 / (2.0 * sigma * sigma * std::log(2.0)))
-                           : std::sqrt((double)kTab / (2.0 * sigma * sigma * std::log(2.0)));
+  // FP32: coordinates scaled so that |dx|^2 is the exponent in units of ln2 (exp2).
+  // FP64: unscaled cell-relative coordinates; kexp = kTab / (2 sigma^2 ln2) converts |dx|^2
+  // to units of ln2/kTab inside the fused range reduction.
+  const double scale = F32 ? std::sqrt(1.0 / (2.0 * sigma * sigma * std::log(2.0))) : 1.0;
+  const double kexp = (double)kTab / (2.0 * sigma * sigma * std::log(2.0));
   k_gauss<DIM, F32><<<P.nitems, kThreads, sm, st>>>(P.g, P.items.get(), t.x, t.y, t.z, t.cell_start,
-                                                    s.x, s.y, s.z, gv, s.cell_start, w, scale, norm, err);
+                                                    s.x, s.y, s.z, gv, s.cell_start, w, scale, kexp, norm, err, skip);
   PRBF_CHECK_LAUNCH();
 }
 
@@ -462,18 +469,18 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
 }
 
 void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv,
-                   double* w, bool fp32, unsigned* err, cudaStream_t st) {
+                   double* w, bool fp32, unsigned* err, cudaStream_t st, const int* skip) {
   if (P.nitems == 0) return;
   if (P.g.dim == 2) {
     if (fp32)
-      launch<2, true>(P, t, s, gv, w, err, st);
+      launch<2, true>(P, t, s, gv, w, err, skip, st);
     else
-      launch<2, false>(P, t, s, gv, w, err, st);
+      launch<2, false>(P, t, s, gv, w, err, skip, st);
   } else {
     if (fp32)
-      launch<3, true>(P, t, s, gv, w, err, st);
+      launch<3, true>(P, t, s, gv, w, err, skip, st);
     else
-      launch<3, false>(P, t, s, gv, w, err, st);
+      launch<3, false>(P, t, s, gv, w, err, skip, st);
   }
 }
 

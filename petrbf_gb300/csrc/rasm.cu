@@ -1,0 +1,764 @@
+// rasm.cu -- restricted additive Schwarz preconditioner on the GPU.
+//
+// Subdomain of cell c = its buffer set (2d/get_buffer.h:9-77: the centre points first,
+// then the neighbour points inside the buffer box), block A_c = phi(|x_i - x_j|) over all
+// pairs of the subdomain, untruncated (mysubmat, 2d/matmult.cxx:53-104). The restricted
+// apply writes only the centre points (is_local = first n_c entries of is,
+// 2d/rbf_interpolation.cxx:214-229):  (B r)[centre(c)] = (A_c^-1 r[buffer(c)])[0:n_c].
+//
+// Two apply forms. Plain FP64: the packed Cholesky factor of every block is kept (about
+// n_b^2/2 doubles per block) and each apply runs a blocked forward substitution plus a
+// back substitution on the centre block only; triangular solves are backward stable, so
+// GMRES reaches the same true residual as with the reference's LU solves. An explicit
+// inverse applied as a GEMV is not: its rounding (eps |A_c^-1| |r|) caps the attainable
+// true residual near 1e-11 on the 2D configurations. Mixed form: S_c = the n_c centre
+// rows of A_c^-1 (n_c x n_b, FP32) once, so an apply is one batched GEMV that streams
+// S_c from HBM; the outer FP64 refinement removes its error. Per block (one CTA):
+//   order the block neighbours first, centre last; K = A_c (2 pi sigma^2) in (0, 1];
+//   left-looking tiled Cholesky K = L L^T (64 x 64 tiles, register-tiled GEMM updates,
+//   each diagonal tile factored and inverted in shared memory);
+//   Y = L^-1 E_centre (only the centre tiles are non-zero);  X = L^-T Y = K^-1 E_centre;
+//   S_c = X^T / (2 pi sigma^2), stored row-major in the block's column order.
+// FP64 for the plain form, FP32 for the mixed form (with a diagonal-shift retry for
+// blocks whose FP32 factorisation meets a non-positive pivot).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "rasm.h"
+
+namespace prbf {
+namespace {
+
+constexpr int TB = 64;         // tile edge
+constexpr int KC = 16;         // inner chunk of the tile GEMM
+constexpr int NTH = 256;       // threads per CTA (16 x 16, 4 x 4 outputs each)
+
+template <class T>
+struct SP {  // padded shared row strides (16-byte aligned rows)
+  static constexpr int S = std::is_same<T, float>::value ? TB + 4 : TB + 2;
+};
+
+// ---- buffer lists ------------------------------------------------------------------
+// One warp per cell. mode 0: count; mode 1: fill idx[boff[c] ...] in order (centre
+// first, then the column ranges of the neighbour window).
+__global__ void k_buffer_lists(Grid g, const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ z, const int* __restrict__ cs, int mode,
+                               int* __restrict__ cnt, const long long* __restrict__ boff,
+                               int* __restrict__ idx) {
+  int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (c >= g.ncell) return;
+  int c0 = cs[c], c1 = cs[c + 1];
+  if (c0 == c1) {  // empty cell: npbufferi = 0 (2d/get_buffer.h:169-171)
+    if (mode == 0 && lane == 0) cnt[c] = 0;
+    return;
+  }
+  int ix, iy, iz;
+  cell_xyz(g, c, ix, iy, iz);
+  double xc = centre_coord(g.xmin, ix, g.box), yc = centre_coord(g.ymin, iy, g.box);
+  double zc = g.dim == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+  double L = g.buffer_len;
+  int nb = g.nb_buffer;
+  int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+  int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+  int jz0 = g.dim == 3 ? max(0, iz - nb) : 0, jz1 = g.dim == 3 ? min(g.nz - 1, iz + nb) : 0;
+  long long pos = mode ? boff[c] : 0;
+  int n = 0;
+  // centre points first
+  for (int j = c0 + lane; j < c1; j += 32)
+    if (mode) idx[pos + (j - c0)] = j;
+  n = c1 - c0;
+  for (int jz = jz0; jz <= jz1; jz++)
+    for (int jx = jx0; jx <= jx1; jx++) {
+      int a = cs[cell_of(g, jx, jy0, jz)], b = cs[cell_of(g, jx, jy1, jz) + 1];
+      for (int j0 = a; j0 < b; j0 += 32) {
+        int j = j0 + lane;
+        bool in = false;
+        if (j < b && !(j >= c0 && j < c1)) {
+          in = fabs(x[j] - xc) < L && fabs(y[j] - yc) < L;
+          if (g.dim == 3) in = in && fabs(z[j] - zc) < L;
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, in);
+        if (mode && in) idx[pos + n + __popc(bal & ((1u << lane) - 1u))] = j;
+        n += __popc(bal);
+      }
+    }
+  if (mode == 0 && lane == 0) cnt[c] = n;
+}
+
+// ---- block assembly ----------------------------------------------------------------
+// K[i][j] = exp(-|x_a - x_b|^2 / (2 sigma^2)) (+ shift on the diagonal), block order
+// neighbours first then centre: block row i < n1 -> buffer entry nc + i, else i - n1.
+// Lower triangle only (the factorisation reads nothing else).
+template <class T>
+__global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const long long* __restrict__ boff,
+                           const int* __restrict__ cs, const int* __restrict__ idx,
+                           const long long* __restrict__ koff, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, int dim, double inv2s2,
+                           double shift, T* __restrict__ K, const unsigned char* __restrict__ only) {
+  int b = blockIdx.y;
+  if (b >= nblk || (only && !only[b])) return;
+  int c = blk_cell[b];
+  int nbk = (int)(boff[c + 1] - boff[c]);
+  int nc = cs[c + 1] - cs[c], n1 = nbk - nc;
+  const int* id = idx + boff[c];
+  T* A = K + koff[b];
+  long long total = (long long)nbk * (nbk + 1) / 2;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    // e -> (i, j), j <= i
+    int i = (int)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
+    while ((long long)i * (i + 1) / 2 > e) i--;
+    while ((long long)(i + 1) * (i + 2) / 2 <= e) i++;
+    int j = (int)(e - (long long)i * (i + 1) / 2);
+    int pa = id[i < n1 ? nc + i : i - n1], pb = id[j < n1 ? nc + j : j - n1];
+    if constexpr (std::is_same<T, float>::value) {
+      // differences in FP64 (coordinates are absolute), exponent in FP32 (SFU exp2)
+      float dx = (float)(x[pa] - x[pb]), dy = (float)(y[pa] - y[pb]);
+      float r2 = dx * dx + dy * dy;
+      if (dim == 3) {
+        float dz = (float)(z[pa] - z[pb]);
+        r2 = fmaf(dz, dz, r2);
+      }
+      float v = exp2f(-r2 * (float)(inv2s2 * 1.4426950408889634));
+      if (i == j) v += (float)shift;
+      A[(long long)i * nbk + j] = v;
+    } else {
+      double dx = x[pa] - x[pb], dy = y[pa] - y[pb];
+      double r2 = dx * dx + dy * dy;
+      if (dim == 3) {
+        double dz = z[pa] - z[pb];
+        r2 += dz * dz;
+      }
+      double v = exp(-r2 * inv2s2);
+      if (i == j) v += shift;
+      A[(long long)i * nbk + j] = v;
+    }
+  }
+}
+
+// ---- tile machinery (one CTA = one block) -------------------------------------------
+template <class T>
+struct Tiles {
+  T* As;  // [KC][S]
+  T* Bs;  // [KC][S]
+  T* C;   // [TB][S] staging tile
+  T* M;   // [TB][S] current diagonal inverse
+};
+
+// Stage a KC x TB chunk of an operand into dst[m][r] (r = output row/col index).
+// src element (r, m) at src[(row0 + r) * ld + col0 + m] if !trans, else
+// src[(row0 + m) * ld + col0 + r]. Out-of-range entries read as zero.
+template <class T>
+__device__ void stage(T* dst, const T* src, long long ld, int row0, int col0, int nr, int nm, bool trans) {
+  constexpr int S = SP<T>::S;
+  for (int e = threadIdx.x; e < KC * TB; e += NTH) {
+    int r, m;
+    if (!trans) {
+      m = e % KC;
+      r = e / KC;
+    } else {
+      r = e % TB;
+      m = e / TB;
+    }
+    T v = T(0);
+    if (r < nr && m < nm) v = trans ? src[(long long)(row0 + m) * ld + col0 + r] : src[(long long)(row0 + r) * ld + col0 + m];
+    dst[m * S + r] = v;
+  }
+}
+
+// acc[4][4] -= sum_m As[m][r] Bs[m][c] over the staged chunk
+template <class T>
+__device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4], int ty, int tx) {
+  constexpr int S = SP<T>::S;
+#pragma unroll
+  for (int m = 0; m < KC; m++) {
+    T a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      a[q] = As[m * S + ty * 4 + q];
+      b[q] = Bs[m * S + tx * 4 + q];
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[p][q] = fma(-a[p], b[q], acc[p][q]);
+  }
+}
+
+// acc -= opA(P) opB(Q) over an inner dimension of length nm (chunks of KC).
+// opA(P)(r, m): P row-major with leading dim ldp, origin (pr, pc), transposed if ta.
+// opB(Q)(c, m): likewise.
+template <class T>
+__device__ void tile_update(Tiles<T>& t, T acc[4][4], const T* P, long long ldp, int pr, int pc, int nr, bool ta,
+                            const T* Q, long long ldq, int qr, int qc, int ncol, bool tb, int nm) {
+  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  for (int m0 = 0; m0 < nm; m0 += KC) {
+    int mm = min(KC, nm - m0);
+    __syncthreads();
+    if (!ta)
+      stage<T>(t.As, P, ldp, pr, pc + m0, nr, mm, false);
+    else
+      stage<T>(t.As, P, ldp, pr + m0, pc, nr, mm, true);
+    if (!tb)
+      stage<T>(t.Bs, Q, ldq, qr, qc + m0, ncol, mm, false);
+    else
+      stage<T>(t.Bs, Q, ldq, qr + m0, qc, ncol, mm, true);
+    __syncthreads();
+    mma_chunk<T>(t.As, t.Bs, acc, ty, tx);
+  }
+}
+
+template <class T>
+__device__ void acc_to_smem(T* C, const T acc[4][4]) {
+  constexpr int S = SP<T>::S;
+  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) C[(ty * 4 + p) * S + tx * 4 + q] = acc[p][q];
+}
+
+// out(r, c) = sum_k L(r, k) R(k, c) over smem tiles, with L = M (lower triangular) or
+// M^T when left is set, and R = C; or out = C M^T when left is false. Result in acc.
+template <class T>
+__device__ void smem_mul(const T* M, const T* C, T acc[4][4], bool left, bool transM) {
+  constexpr int S = SP<T>::S;
+  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[p][q] = T(0);
+  for (int k = 0; k < TB; k++) {
+    T a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int r = ty * 4 + q, c = tx * 4 + q;
+      if (left) {
+        a[q] = transM ? M[k * S + r] : M[r * S + k];
+        b[q] = C[k * S + c];
+      } else {  // C M^T: (r, c) = sum_k C(r, k) M(c, k)
+        a[q] = C[r * S + k];
+        b[q] = M[c * S + k];
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+  }
+}
+
+// In-place Cholesky of the h x h leading part of C (lower), then its inverse into M.
+// Returns false if a pivot is not positive. Entries outside h x h are set to identity.
+template <class T>
+__device__ bool potrf_trtri(T* C, T* M, int h) {
+  constexpr int S = SP<T>::S;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < TB * TB; e += NTH) {
+    int r = e / TB, c = e % TB;
+    if (r >= h || c >= h) C[r * S + c] = (r == c) ? T(1) : T(0);
+    if (c > r) C[r * S + c] = T(0);
+  }
+  __syncthreads();
+  for (int j = 0; j < h; j++) {
+    T d = C[j * S + j];
+    if (!(d > T(0))) {
+      if (threadIdx.x == 0) s_bad = 1;
+      d = T(1);
+    }
+    T s = sqrt(d);
+    __syncthreads();
+    // column j below the diagonal, then the rank-1 update of the trailing lower part
+    for (int i = j + 1 + threadIdx.x; i < h; i += NTH) C[i * S + j] /= s;
+    __syncthreads();
+    if (threadIdx.x == 0) C[j * S + j] = s;
+    int rem = h - j - 1;
+    for (int e = threadIdx.x; e < rem * rem; e += NTH) {
+      int i = j + 1 + e / rem, l = j + 1 + e % rem;
+      if (l <= i) C[i * S + l] = fma(-C[i * S + j], C[l * S + j], C[i * S + l]);
+    }
+    __syncthreads();
+  }
+  // M = C^-1 (lower triangular), column by column: thread c owns column c
+  for (int e = threadIdx.x; e < TB * TB; e += NTH) M[(e / TB) * S + (e % TB)] = T(0);
+  __syncthreads();
+  if (threadIdx.x < TB) {
+    int c = threadIdx.x;
+    M[c * S + c] = T(1) / C[c * S + c];
+    for (int r = c + 1; r < TB; r++) {
+      T s = T(0);
+      for (int k = c; k < r; k++) s = fma(C[r * S + k], M[k * S + c], s);
+      M[r * S + c] = -s / C[r * S + r];
+    }
+  }
+  __syncthreads();
+  return s_bad == 0;
+}
+
+template <class T>
+__device__ void store_acc(T* dst, long long ld, int r0, int c0, int nr, int nc, const T acc[4][4]) {
+  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int r = ty * 4 + p, c = tx * 4 + q;
+      if (r < nr && c < nc) dst[(long long)(r0 + r) * ld + c0 + c] = acc[p][q];
+    }
+}
+
+template <class T>
+__device__ void load_acc(const T* src, long long ld, int r0, int c0, int nr, int nc, T acc[4][4], bool lower_only) {
+  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int r = ty * 4 + p, c = tx * 4 + q;
+      bool ok = r < nr && c < nc && (!lower_only || (r0 + r) >= (c0 + c));
+      acc[p][q] = ok ? src[(long long)(r0 + r) * ld + c0 + c] : T(0);
+    }
+}
+
+// Tile boundaries: neighbour part [0, n1) in TB steps, centre part [n1, nb) in TB steps.
+__device__ __forceinline__ void tile_range(int t, int n1, int nb, int kc1, int& r0, int& h) {
+  if (t < kc1) {
+    r0 = t * TB;
+    h = min(TB, n1 - r0);
+  } else {
+    r0 = n1 + (t - kc1) * TB;
+    h = min(TB, nb - r0);
+  }
+}
+
+// One CTA per block: Cholesky, centre columns of the inverse, S_c.
+template <class T>
+__global__ void __launch_bounds__(NTH) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
+                                                 const long long* __restrict__ boff, const int* __restrict__ cs,
+                                                 const long long* __restrict__ koff, T* __restrict__ K,
+                                                 const long long* __restrict__ xoff, T* __restrict__ Xw,
+                                                 const long long* __restrict__ soff, T* __restrict__ Sout,
+                                                 double out_scale, unsigned char* __restrict__ bad,
+                                                 const unsigned char* __restrict__ only, int mode,
+                                                 const long long* __restrict__ loff, T* __restrict__ Lpack) {
+  int b = blockIdx.x;
+  if (b >= nblk || (only && !only[b])) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int S = SP<T>::S;
+  Tiles<T> t;
+  t.As = (T*)smem_raw;
+  t.Bs = t.As + KC * S;
+  t.C = t.Bs + KC * S;
+  t.M = t.C + TB * S;
+  T* Minv_all = nullptr;  // diagonal inverses live in Xw after X (see xoff layout)
+  int c = blk_cell[b];
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
+  const int kc1 = (n1 + TB - 1) / TB;           // neighbour tiles
+  const int ntile = kc1 + (nc + TB - 1) / TB;   // all tiles
+  const int nct = ntile - kc1;                  // centre tiles
+  T* A = K + koff[b];
+  T* X = Xw + xoff[b];                   // nb x (nct*TB), row-major
+  const long long ldx = (long long)nct * TB;
+  Minv_all = X + (long long)nb * ldx;    // ntile diagonal inverses, TB x TB each
+  bool ok = true;
+
+  // ---- Cholesky, left-looking over tile columns -------------------------------------
+  for (int k = 0; k < ntile; k++) {
+    int rk, hk;
+    tile_range(k, n1, nb, kc1, rk, hk);
+    for (int i = k; i < ntile; i++) {
+      int ri, hi;
+      tile_range(i, n1, nb, kc1, ri, hi);
+      T acc[4][4];
+      load_acc<T>(A, nb, ri, rk, hi, hk, acc, true);
+      for (int p = 0; p < k; p++) {
+        int rp, hp;
+        tile_range(p, n1, nb, kc1, rp, hp);
+        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, A, nb, rk, rp, hk, false, hp);
+      }
+      __syncthreads();
+      acc_to_smem<T>(t.C, acc);
+      __syncthreads();
+      if (i == k) {
+        ok = potrf_trtri<T>(t.C, t.M, hk) && ok;
+        // store L_kk (lower part) and, for the S_c phases, its inverse
+        for (int e = threadIdx.x; e < TB * TB; e += NTH) {
+          int r = e / TB, cc = e % TB;
+          if (r < hk && cc <= r) A[(long long)(rk + r) * nb + rk + cc] = t.C[r * S + cc];
+          if (mode == 0) Minv_all[(long long)k * TB * TB + e] = t.M[r * S + cc];
+        }
+        __syncthreads();
+      } else {
+        T out[4][4];
+        smem_mul<T>(t.M, t.C, out, false, false);  // C * Minv^T
+        store_acc<T>(A, nb, ri, rk, hi, hk, out);
+      }
+      __syncthreads();
+    }
+  }
+
+  if (mode == 1) {
+    // keep the factor: rows of the lower triangle, row i holding L[i][0..i], scaled so
+    // that it factors A = K / (2 pi sigma^2): L_A = L_K sqrt(1 / (2 pi sigma^2))
+    T* Lp = Lpack + loff[c];
+    const T sc = (T)out_scale;
+    for (int i = 0; i < nb; i++) {
+      long long o = (long long)i * (i + 1) / 2;
+      for (int j = threadIdx.x; j <= i; j += NTH) Lp[o + j] = A[(long long)i * nb + j] * sc;
+    }
+    if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
+    return;
+  }
+  // ---- forward: Y = L^-1 E_centre (centre tiles only), stored in X -------------------
+  for (int i = kc1; i < ntile; i++) {
+    int ri, hi;
+    tile_range(i, n1, nb, kc1, ri, hi);
+    // diagonal inverse of tile i into M
+    for (int e = threadIdx.x; e < TB * TB; e += NTH) t.M[(e / TB) * S + e % TB] = Minv_all[(long long)i * TB * TB + e];
+    for (int cj = 0; cj < nct; cj++) {
+      int j = kc1 + cj;
+      if (j > i) break;
+      T acc[4][4];
+#pragma unroll
+      for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[p][q] = T(0);
+      if (j == i) {
+        int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+#pragma unroll
+        for (int p = 0; p < 4; p++) acc[p][p] = (tx == ty) ? T(1) : T(0);
+      }
+      for (int p = j; p < i; p++) {  // acc -= L[i,p] Y[p, cj]
+        int rp, hp;
+        tile_range(p, n1, nb, kc1, rp, hp);
+        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, X, ldx, rp, cj * TB, TB, true, hp);
+      }
+      __syncthreads();
+      acc_to_smem<T>(t.C, acc);
+      __syncthreads();
+      T out[4][4];
+      smem_mul<T>(t.M, t.C, out, true, false);  // Minv * acc
+      store_acc<T>(X, ldx, ri, cj * TB, hi, TB, out);
+      __syncthreads();
+    }
+  }
+  // ---- back: X = L^-T Y, tile rows from the bottom; Y = 0 above the centre ------------
+  for (int i = ntile - 1; i >= 0; i--) {
+    int ri, hi;
+    tile_range(i, n1, nb, kc1, ri, hi);
+    for (int e = threadIdx.x; e < TB * TB; e += NTH) t.M[(e / TB) * S + e % TB] = Minv_all[(long long)i * TB * TB + e];
+    for (int cj = 0; cj < nct; cj++) {
+      T acc[4][4];
+      int cjt = kc1 + cj;
+      if (i >= kc1 && cjt <= i)
+        load_acc<T>(X, ldx, ri, cj * TB, hi, TB, acc, false);
+      else {
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[p][q] = T(0);
+      }
+      for (int j = i + 1; j < ntile; j++) {  // acc -= L[j,i]^T X[j, cj]
+        int rj, hj;
+        tile_range(j, n1, nb, kc1, rj, hj);
+        tile_update<T>(t, acc, A, nb, rj, ri, hi, true, X, ldx, rj, cj * TB, TB, true, hj);
+      }
+      __syncthreads();
+      acc_to_smem<T>(t.C, acc);
+      __syncthreads();
+      T out[4][4];
+      smem_mul<T>(t.M, t.C, out, true, true);  // Minv^T * acc
+      __syncthreads();
+      store_acc<T>(X, ldx, ri, cj * TB, hi, TB, out);
+      __syncthreads();
+    }
+  }
+  // ---- S_c[r][j] = X[j][centre col r] * out_scale, r < nc, j < nb -----------------------
+  T* Sc = Sout + soff[c];
+  for (long long e = threadIdx.x; e < (long long)nc * nb; e += NTH) {
+    int r = (int)(e / nb), j = (int)(e % nb);
+    Sc[e] = (T)((double)X[(long long)j * ldx + r] * out_scale);
+  }
+  if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
+}
+
+// ---- apply: out[centre(c)] = S_c r[buffer(c) in block order] --------------------------
+template <class T>
+__global__ void __launch_bounds__(128) k_apply(int ncell, const long long* __restrict__ boff,
+                                               const int* __restrict__ cs, const int* __restrict__ idx,
+                                               const long long* __restrict__ soff, const T* __restrict__ S,
+                                               const double* __restrict__ r, double* __restrict__ out,
+                                               const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* rv = (T*)smem_raw;
+  int c = blockIdx.x;
+  int nb = (int)(boff[c + 1] - boff[c]);
+  if (nb == 0) return;
+  int nc = cs[c + 1] - cs[c], n1 = nb - nc;
+  const int* id = idx + boff[c];
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) rv[j] = (T)r[id[j < n1 ? nc + j : j - n1]];
+  __syncthreads();
+  const T* Sc = S + soff[c];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int row = w; row < nc; row += nw) {
+    const T* sr = Sc + (long long)row * nb;
+    T s = T(0);
+    for (int j = lane; j < nb; j += 32) s = fma(sr[j], rv[j], s);
+    s = warp_sum(s);
+    if (lane == 0) out[cs[c] + row] = (double)s;
+  }
+}
+
+// ---- apply with the factor: out[centre(c)] = (L^-T L^-1 r_c)[centre] ----------------
+// Forward substitution over the whole block (32-row panels: warp 0 solves the diagonal
+// triangle from shared memory, all warps update the rows below with coalesced row
+// segments), then the back substitution with L22^T only, since the centre unknowns are
+// the last n_c: x2 = L22^-T y2.
+template <class T>
+__global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* __restrict__ boff,
+                                                   const int* __restrict__ cs, const int* __restrict__ idx,
+                                                   const long long* __restrict__ loff, const T* __restrict__ Lpack,
+                                                   const double* __restrict__ r, double* __restrict__ out,
+                                                   const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tri[32][33];
+  T* y = (T*)smem_raw;
+  const int c = blockIdx.x;
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  if (nb == 0) return;
+  const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
+  const int* id = idx + boff[c];
+  const T* L = Lpack + loff[c];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  for (int j = tid; j < nb; j += blockDim.x) y[j] = (T)r[id[j < n1 ? nc + j : j - n1]];
+  __syncthreads();
+  // forward: L y = r
+  for (int p0 = 0; p0 < nb; p0 += 32) {
+    const int np = min(32, nb - p0);
+    for (int e = tid; e < 32 * 32; e += blockDim.x) {
+      int i = e >> 5, j = e & 31;
+      tri[i][j] = (i < np && j <= i) ? L[(long long)(p0 + i) * (p0 + i + 1) / 2 + p0 + j] : T(0);
+    }
+    __syncthreads();
+    if (w == 0) {
+      T ri = lane < np ? y[p0 + lane] : T(0);
+      for (int j = 0; j < np; j++) {
+        if (lane == j) ri = ri / tri[j][j];
+        T yj = __shfl_sync(0xffffffffu, ri, j);
+        if (lane > j) ri = fma(-tri[lane][j], yj, ri);
+      }
+      if (lane < np) y[p0 + lane] = ri;
+    }
+    __syncthreads();
+    const T yl = lane < np ? y[p0 + lane] : T(0);
+    for (int i = p0 + np + w; i < nb; i += nw) {
+      T v = lane < np ? L[(long long)i * (i + 1) / 2 + p0 + lane] * yl : T(0);
+      v = warp_sum(v);
+      if (lane == 0) y[i] -= v;
+    }
+    __syncthreads();
+  }
+  // backward on the centre block: L22^T x2 = y2, panels from the bottom
+  T* y2 = y + n1;
+  for (int pe = nc; pe > 0; pe -= 32) {
+    const int p0 = max(0, pe - 32), np = pe - p0;
+    // tri[i][j] = L22[p0 + i][p0 + j], j <= i
+    for (int e = tid; e < 32 * 32; e += blockDim.x) {
+      int i = e >> 5, j = e & 31;
+      long long row = n1 + p0 + i;
+      tri[i][j] = (i < np && j <= i) ? L[row * (row + 1) / 2 + n1 + p0 + j] : T(0);
+    }
+    __syncthreads();
+    if (w == 0) {  // x_i = (y_i - sum_{j > i} L22[j][i] x_j) / L22[i][i], i = np-1 .. 0
+      T xi = lane < np ? y2[p0 + lane] : T(0);
+      for (int j = np - 1; j >= 0; j--) {
+        if (lane == j) xi = xi / tri[j][j];
+        T xj = __shfl_sync(0xffffffffu, xi, j);
+        if (lane < j) xi = fma(-tri[j][lane], xj, xi);
+      }
+      if (lane < np) y2[p0 + lane] = xi;
+    }
+    __syncthreads();
+    // rows above the panel: y2[k] -= sum_{j in panel} L22[p0 + j][k] x_j, k < p0
+    for (int k = tid; k < p0; k += blockDim.x) {
+      T acc = T(0);
+      for (int j = 0; j < np; j++) {
+        long long row = n1 + p0 + j;
+        acc = fma(L[row * (row + 1) / 2 + n1 + k], y2[p0 + j], acc);
+      }
+      y2[k] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < nc; i += blockDim.x) out[cs[c] + i] = (double)y2[i];
+}
+
+template <class T>
+size_t chol_smem() {
+  return sizeof(T) * (2 * KC * SP<T>::S + 2 * TB * SP<T>::S);
+}
+
+}  // namespace
+
+void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsigned* err, cudaStream_t s,
+                double ws_budget_bytes) {
+  (void)err;
+  const Grid& g = P.g;
+  R.fp32 = fp32;
+  R.ncell = g.ncell;
+  int* cnt = (int*)ws.get(40, sizeof(int) * ((size_t)g.ncell + 1));
+  k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(), 0, cnt,
+                                                      nullptr, nullptr);
+  PRBF_CHECK_LAUNCH();
+  std::vector<int> hcnt(g.ncell), hcs(g.ncell + 1);
+  PRBF_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, sizeof(int) * g.ncell, cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaMemcpyAsync(hcs.data(), P.cs.get(), sizeof(int) * (g.ncell + 1), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  // host plan: offsets of buffer lists and S_c, the list of non-empty blocks
+  std::vector<long long> hb(g.ncell + 1), hso(g.ncell + 1);
+  std::vector<int> blk;
+  hb[0] = hso[0] = 0;
+  R.max_nb = 0;
+  R.max_nc = 0;
+  for (int c = 0; c < g.ncell; c++) {
+    long long nbk = hcnt[c], nc = hcs[c + 1] - hcs[c];
+    hb[c + 1] = hb[c] + nbk;
+    hso[c + 1] = hso[c] + nbk * nc;
+    if (nbk) blk.push_back(c);
+    R.max_nb = std::max<int>(R.max_nb, (int)nbk);
+    R.max_nc = std::max<int>(R.max_nc, (int)nc);
+  }
+  R.nblocks = (int)blk.size();
+  R.boff.reserve(g.ncell + 1);
+  R.soff.reserve(g.ncell + 1);
+  R.idx.reserve(std::max<long long>(hb[g.ncell], 1));
+  PRBF_CUDA(cudaMemcpyAsync(R.boff.get(), hb.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyAsync(R.soff.get(), hso.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
+  k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(), 1, cnt,
+                                                      R.boff.get(), R.idx.get());
+  PRBF_CHECK_LAUNCH();
+  size_t esz = fp32 ? sizeof(float) : sizeof(double);
+  // FP64 form keeps the packed Cholesky factors (backward-stable triangular solves at
+  // every apply); the FP32 form keeps S_c (one GEMV per apply)
+  R.factor = !fp32;
+  if (R.factor) {
+    std::vector<long long> hl(g.ncell + 1);
+    hl[0] = 0;
+    for (int c = 0; c < g.ncell; c++) hl[c + 1] = hl[c] + (long long)hcnt[c] * (hcnt[c] + 1) / 2;
+    R.loff.reserve(g.ncell + 1);
+    PRBF_CUDA(cudaMemcpyAsync(R.loff.get(), hl.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
+    R.L64.reserve(std::max<long long>(hl[g.ncell], 1));
+    PRBF_CUDA(cudaStreamSynchronize(s));
+  } else {
+    R.S32.reserve(std::max<long long>(hso[g.ncell], 1));
+  }
+
+  // batches of blocks within the workspace budget: K (nb^2), X (nb x ceil(nc/TB)TB) and
+  // the diagonal inverses (ntile TB^2)
+  const double inv2s2 = 1.0 / (2.0 * g.sigma * g.sigma);
+  const double out_scale = 2.0 * M_PI * g.sigma * g.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
+  size_t smem = fp32 ? chol_smem<float>() : chol_smem<double>();
+  if (fp32)
+    PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  else
+    PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  R.nfallback = 0;
+  size_t pos = 0;
+  std::vector<long long> hk, hx;
+  std::vector<int> bc;
+  std::vector<unsigned char> hbad;
+  while (pos < blk.size()) {
+    hk.assign(1, 0);
+    hx.assign(1, 0);
+    bc.clear();
+    size_t q = pos;
+    while (q < blk.size()) {
+      int c = blk[q];
+      long long nbk = hcnt[c], nc = hcs[c + 1] - hcs[c];
+      long long n1 = nbk - nc;
+      long long ntile = (n1 + TB - 1) / TB + (nc + TB - 1) / TB;
+      long long nct = (nc + TB - 1) / TB;
+      long long ke = nbk * nbk, xe = fp32 ? nbk * nct * TB + ntile * TB * TB : 1;
+      if (!bc.empty() && (double)(hk.back() + ke + hx.back() + xe) * esz > ws_budget_bytes) break;
+      bc.push_back(c);
+      hk.push_back(hk.back() + ke);
+      hx.push_back(hx.back() + xe);
+      q++;
+    }
+    int nb_batch = (int)bc.size();
+    int* dbc = (int*)ws.get(41, sizeof(int) * nb_batch);
+    long long* dk = (long long*)ws.get(42, sizeof(long long) * (nb_batch + 1));
+    long long* dx = (long long*)ws.get(43, sizeof(long long) * (nb_batch + 1));
+    unsigned char* dbad = (unsigned char*)ws.get(44, nb_batch);
+    void* Kw = ws.get(45, (size_t)hk.back() * esz);
+    void* Xw = ws.get(46, (size_t)hx.back() * esz);
+    PRBF_CUDA(cudaMemcpyAsync(dbc, bc.data(), sizeof(int) * nb_batch, cudaMemcpyHostToDevice, s));
+    PRBF_CUDA(cudaMemcpyAsync(dk, hk.data(), sizeof(long long) * (nb_batch + 1), cudaMemcpyHostToDevice, s));
+    PRBF_CUDA(cudaMemcpyAsync(dx, hx.data(), sizeof(long long) * (nb_batch + 1), cudaMemcpyHostToDevice, s));
+    const double* zp = P.view().z;
+    for (int attempt = 0; attempt < 3; attempt++) {
+      const unsigned char* only = attempt ? dbad : nullptr;
+      // diagonal shift of the retries (relative to the unit diagonal of K)
+      double shift = attempt == 0 ? 0.0 : (fp32 ? (attempt == 1 ? 1e-5 : 1e-3) : (attempt == 1 ? 1e-12 : 1e-9));
+      dim3 ag(64, nb_batch);
+      if (fp32) {
+        k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
+                                             P.y.get(), zp, g.dim, inv2s2, shift, (float*)Kw, only);
+        PRBF_CHECK_LAUNCH();
+        k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
+                                                     (float*)Xw, R.soff.get(), R.S32.get(), out_scale, dbad,
+                                                     only, 0, nullptr, nullptr);
+      } else {
+        k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
+                                              P.y.get(), zp, g.dim, inv2s2, shift, (double*)Kw, only);
+        PRBF_CHECK_LAUNCH();
+        k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (double*)Kw, dx,
+                                                      (double*)Xw, R.soff.get(), nullptr,
+                                                      std::sqrt(1.0 / out_scale), dbad, only, 1, R.loff.get(),
+                                                      R.L64.get());
+      }
+      PRBF_CHECK_LAUNCH();
+      hbad.resize(nb_batch);
+      PRBF_CUDA(cudaMemcpyAsync(hbad.data(), dbad, nb_batch, cudaMemcpyDeviceToHost, s));
+      PRBF_CUDA(cudaStreamSynchronize(s));
+      int nbad = 0;
+      for (unsigned char v : hbad) nbad += v ? 1 : 0;
+      if (nbad == 0) break;
+      if (attempt == 2) throw Error(PRBF_ERR_FACTOR, "subdomain block not positive definite after shifted retries");
+      R.nfallback += nbad;
+    }
+    pos = q;
+  }
+}
+
+void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s, const int* skip) {
+  if (R.nblocks == 0) return;
+  size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
+  if (R.factor)
+    k_apply_tri<double><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L64.get(), r,
+                                                 out, skip);
+  else
+    k_apply<float><<<R.ncell, 128, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.soff.get(), R.S32.get(), r, out,
+                                            skip);
+  PRBF_CHECK_LAUNCH();
+}
+
+void rasm_set_apply_smem(const RasmPlan& R) {
+  size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
+  if (sm > 48 * 1024) {
+    if (sm > 200 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
+    if (R.factor)
+      PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    else
+      PRBF_CUDA(cudaFuncSetAttribute(k_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  }
+}
+
+}  // namespace prbf

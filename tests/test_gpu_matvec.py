@@ -54,7 +54,9 @@ def test_matvec_fp64_matches_reference(golden, case):
         y = c.matvec(v)[perm]
     ref = d["matvec_out"]
     assert _rel(y, ref) <= RTOL_FP64
-    np.testing.assert_allclose(y, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    # per-term accuracy at the reference's level: only the summation order differs
+    assert _rel(y, ref) <= 1e-14
+    np.testing.assert_allclose(y, ref, rtol=0, atol=1e-14 * np.abs(ref).max())
 
 
 @pytest.mark.parametrize("case", CASES)
