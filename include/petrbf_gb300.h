@@ -144,6 +144,30 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
                           float* wg, int np, float* xp, float* yp, float* zp, float* gp,
                           float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc);
 
+/* Cell sort that allocates nothing (no counterpart in the reference). For callers that
+ * must not allocate device memory themselves -- an application that reserves the whole
+ * GPU for its own memory pool, or a latency-critical loop that cannot afford the device
+ * synchronisation cudaMalloc/cudaFree imply -- it sorts n points into the same cells, in
+ * the same order, as prbf_matvec_setup: perm_dev[k] = caller index of the k-th sorted
+ * point, cell_start_dev[c] = first sorted position of cell c (ncell + 1 entries; the grid
+ * is derived from the points' bounding box, so the caller passes the capacity it
+ * allocated and receives ncell). All pointers are device pointers; stream may be null.
+ * Every temporary comes from one fixed device array inside the library
+ * (PRBF_STATIC_SORT_SCRATCH_MIB MiB, held on every GPU that loads the library until the
+ * process exits). Limits: n <= PRBF_STATIC_SORT_MAX_POINTS and ncell + 1 <= 8,388,608;
+ * beyond them the call returns PRBF_ERR_CAPACITY without touching the buffers. The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture. All calls share the
+ * array: calls that overlap on the GPU (other threads, other streams) race and must be
+ * serialised by the caller. The call synchronises the stream once to read the bounding
+ * box back. */
+#define PRBF_STATIC_SORT_MAX_POINTS 1048576
+#define PRBF_STATIC_SORT_SCRATCH_MIB 13
+int prbf_cell_sort_static(int dim, int n, const double* x_dev, const double* y_dev, const double* z_dev,
+                          double sigma, int nsigma_box, int sigma_buffer, int sigma_trunc,
+                          int* perm_dev, int* cell_start_dev, int cell_start_len, int* ncell_out,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,10 @@ SIGNATURES = {
     "prbf_get_trunc_counts": (ctypes.c_int, [ctypes.c_void_p, _I]),
     "prbf_pc_setup": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "prbf_pc_apply": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
+    "prbf_cell_sort_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
     "prbf_RBFInterpolation": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _F, _F, _F,
                                              _F, ctypes.c_int, _F, _F, _F, _F, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int]),

@@ -307,3 +307,138 @@ void scatter_dev(int n, const int* perm, const double* in, double* out, cudaStre
 }
 
 }  // namespace prbf
+
+// ---- cell sort without allocation -------------------------------------------------------
+// prbf_cell_sort_static (declared in include/petrbf_gb300.h) sorts into caller-provided
+// device buffers and takes every temporary from one fixed device array of this file, so
+// it never calls cudaMalloc or cudaFree. The array lives on every GPU that loads the
+// library until the process exits; all calls share it.
+#include <mutex>
+
+#include "context.h"
+
+namespace prbf {
+namespace {
+
+constexpr int kStaticMaxPoints = PRBF_STATIC_SORT_MAX_POINTS;
+constexpr long long kStaticMaxScan = 2048LL * 4096;  // entries a two-level scan can take
+constexpr int kStaticTiles = (kStaticMaxPoints + kRadixTile - 1) / kRadixTile;
+// byte offsets inside the scratch array (each 256-aligned)
+constexpr size_t kOffKeyA = 0;
+constexpr size_t kOffKeyB = kOffKeyA + sizeof(unsigned) * (size_t)kStaticMaxPoints;
+constexpr size_t kOffValB = kOffKeyB + sizeof(unsigned) * (size_t)kStaticMaxPoints;
+constexpr size_t kOffHist = kOffValB + sizeof(int) * (size_t)kStaticMaxPoints;
+constexpr size_t kOffSums1 = kOffHist + sizeof(int) * 256 * (size_t)kStaticTiles;
+constexpr size_t kOffSums2 = kOffSums1 + sizeof(int) * 4096;
+constexpr size_t kOffBboxPart = kOffSums2 + 256;
+constexpr size_t kOffBbox = kOffBboxPart + sizeof(double) * 6 * kBboxBlocks;
+constexpr size_t kOffErr = kOffBbox + 256;
+constexpr size_t kStaticScratchBytes = kOffErr + 256;
+
+static __device__ __align__(256) unsigned char g_static_sort_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char* g_static_addr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array for the current device, looked up once per device.
+int static_scratch(unsigned char** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PRBF_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_sort_scratch) != cudaSuccess || !p) return PRBF_ERR_CUDA;
+    g_static_addr[dev] = (unsigned char*)p;
+  }
+  *out = g_static_addr[dev];
+  return PRBF_OK;
+}
+
+// Exclusive scan of n <= kStaticMaxScan ints with the partial sums in the scratch array.
+void static_scan(int* data, long long n, int* sums1, int* sums2, cudaStream_t s) {
+  long long nb1 = (n + kScanTile - 1) / kScanTile;
+  if (nb1 == 1) {
+    k_scan_tiles<int><<<1, kScanThreads, 0, s>>>(data, data, nullptr, n);
+    return;
+  }
+  k_scan_tiles<int><<<(unsigned)nb1, kScanThreads, 0, s>>>(data, data, sums1, n);
+  long long nb2 = (nb1 + kScanTile - 1) / kScanTile;
+  if (nb2 == 1) {
+    k_scan_tiles<int><<<1, kScanThreads, 0, s>>>(sums1, sums1, nullptr, nb1);
+  } else {
+    k_scan_tiles<int><<<(unsigned)nb2, kScanThreads, 0, s>>>(sums1, sums1, sums2, nb1);
+    k_scan_tiles<int><<<1, kScanThreads, 0, s>>>(sums2, sums2, nullptr, nb2);
+    k_scan_add<int><<<(unsigned)nb2, kScanThreads, 0, s>>>(sums1, sums2, nb1);
+  }
+  k_scan_add<int><<<(unsigned)nb1, kScanThreads, 0, s>>>(data, sums1, n);
+}
+
+}  // namespace
+}  // namespace prbf
+
+extern "C" int prbf_cell_sort_static(int dim, int n, const double* x, const double* y, const double* z,
+                                     double sigma, int nsigma_box, int sigma_buffer, int sigma_trunc,
+                                     int* perm, int* cell_start, int cell_start_len, int* ncell_out,
+                                     void* stream) {
+  using namespace prbf;
+  if ((dim != 2 && dim != 3) || n <= 0 || !x || !y || (dim == 3 && !z) || !perm || !cell_start ||
+      cell_start_len <= 0)
+    return PRBF_ERR_ARG;
+  if (n > kStaticMaxPoints) return PRBF_ERR_CAPACITY;  // beyond the fixed scratch array
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char* base = nullptr;
+  int st = static_scratch(&base);
+  if (st) return st;
+  unsigned* keyA = (unsigned*)(base + kOffKeyA);
+  unsigned* keyB = (unsigned*)(base + kOffKeyB);
+  int* valB = (int*)(base + kOffValB);
+  int* hist = (int*)(base + kOffHist);
+  int* sums1 = (int*)(base + kOffSums1);
+  int* sums2 = (int*)(base + kOffSums2);
+  double* bpart = (double*)(base + kOffBboxPart);
+  double* bbox = (double*)(base + kOffBbox);
+  unsigned* err = (unsigned*)(base + kOffErr);
+  try {
+    // the error word is the only scratch that must start at zero
+    PRBF_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), s));
+    int blocks = std::min(kBboxBlocks, std::max(1, ceil_div(n, kBboxThreads)));
+    k_bbox_partial<<<blocks, kBboxThreads, 0, s>>>(n, x, y, dim == 3 ? z : nullptr, bpart);
+    k_bbox_final<<<1, 32, 0, s>>>(blocks, bpart, bbox);
+    PRBF_CHECK_LAUNCH();
+    double b[6];
+    PRBF_CUDA(cudaMemcpyAsync(b, bbox, sizeof(b), cudaMemcpyDeviceToHost, s));
+    PRBF_CUDA(cudaStreamSynchronize(s));
+    Grid g = make_grid(dim, b, sigma, nsigma_box, sigma_buffer, sigma_trunc);
+    if ((long long)g.ncell + 1 > cell_start_len || (long long)g.ncell + 1 > kStaticMaxScan)
+      return PRBF_ERR_CAPACITY;
+    PRBF_CUDA(cudaMemsetAsync(cell_start, 0, sizeof(int) * ((size_t)g.ncell + 1), s));
+    k_cell_ids<<<ceil_div(n, 256), 256, 0, s>>>(g, n, x, y, dim == 3 ? z : nullptr, keyA, perm, cell_start, err);
+    PRBF_CHECK_LAUNCH();
+    static_scan(cell_start, (long long)g.ncell + 1, sums1, sums2, s);
+    int bits = 0;
+    while (bits < 31 && (1u << bits) < (unsigned)g.ncell) bits++;
+    int passes = (bits + 7) / 8;
+    int ntiles = ceil_div(n, kRadixTile);
+    unsigned *kin = keyA, *kout = keyB;
+    int *vin = perm, *vout = valB;
+    for (int p = 0; p < passes; p++) {
+      k_radix_hist<<<ntiles, kRadixThreads, 0, s>>>(kin, n, 8 * p, hist, ntiles);
+      static_scan(hist, 256LL * ntiles, sums1, sums2, s);
+      k_radix_scatter<<<ntiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, n, 8 * p, hist, ntiles);
+      PRBF_CHECK_LAUNCH();
+      std::swap(kin, kout);
+      std::swap(vin, vout);
+    }
+    if (vin != perm)
+      PRBF_CUDA(cudaMemcpyAsync(perm, vin, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    unsigned herr = 0;
+    PRBF_CUDA(cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    PRBF_CUDA(cudaStreamSynchronize(s));
+    if (herr & DEV_ERR_RANGE) return PRBF_ERR_RANGE;
+    if (ncell_out) *ncell_out = g.ncell;
+    return PRBF_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}
