@@ -31,8 +31,13 @@ namespace prbf {
 namespace {
 
 constexpr int TB = 64;         // tile edge
-constexpr int KC = 16;         // inner chunk of the tile GEMM
 constexpr int NTH = 256;       // threads per CTA (16 x 16, 4 x 4 outputs each)
+// inner chunk of the tile GEMM: FP32 is latency-bound on its operand loads, so it takes
+// wider chunks; FP64 is bound by the FP64 pipe and keeps shared memory small
+template <class T>
+struct KCOf {
+  static constexpr int v = std::is_same<T, float>::value ? 32 : 16;
+};
 
 template <class T>
 struct SP {  // padded shared row strides (16-byte aligned rows)
@@ -104,36 +109,33 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
   int nc = cs[c + 1] - cs[c], n1 = nbk - nc;
   const int* id = idx + boff[c];
   T* A = K + koff[b];
-  long long total = (long long)nbk * (nbk + 1) / 2;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    // e -> (i, j), j <= i
-    int i = (int)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
-    while ((long long)i * (i + 1) / 2 > e) i--;
-    while ((long long)(i + 1) * (i + 2) / 2 <= e) i++;
-    int j = (int)(e - (long long)i * (i + 1) / 2);
-    int pa = id[i < n1 ? nc + i : i - n1], pb = id[j < n1 ? nc + j : j - n1];
-    if constexpr (std::is_same<T, float>::value) {
-      // differences in FP64 (coordinates are absolute), exponent in FP32 (SFU exp2)
-      float dx = (float)(x[pa] - x[pb]), dy = (float)(y[pa] - y[pb]);
-      float r2 = dx * dx + dy * dy;
-      if (dim == 3) {
-        float dz = (float)(z[pa] - z[pb]);
-        r2 = fmaf(dz, dz, r2);
+  for (int i = blockIdx.x; i < nbk; i += gridDim.x) {
+    const int pa = id[i < n1 ? nc + i : i - n1];
+    const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+      const int pb = id[j < n1 ? nc + j : j - n1];
+      if constexpr (std::is_same<T, float>::value) {
+        // differences in FP64 (coordinates are absolute), exponent in FP32 (SFU exp2)
+        float dx = (float)(xa - x[pb]), dy = (float)(ya - y[pb]);
+        float r2 = dx * dx + dy * dy;
+        if (dim == 3) {
+          float dz = (float)(za - z[pb]);
+          r2 = fmaf(dz, dz, r2);
+        }
+        float v = exp2f(-r2 * (float)(inv2s2 * 1.4426950408889634));
+        if (i == j) v += (float)shift;
+        A[(long long)i * nbk + j] = v;
+      } else {
+        double dx = xa - x[pb], dy = ya - y[pb];
+        double r2 = dx * dx + dy * dy;
+        if (dim == 3) {
+          double dz = za - z[pb];
+          r2 += dz * dz;
+        }
+        double v = exp(-r2 * inv2s2);
+        if (i == j) v += shift;
+        A[(long long)i * nbk + j] = v;
       }
-      float v = exp2f(-r2 * (float)(inv2s2 * 1.4426950408889634));
-      if (i == j) v += (float)shift;
-      A[(long long)i * nbk + j] = v;
-    } else {
-      double dx = x[pa] - x[pb], dy = y[pa] - y[pb];
-      double r2 = dx * dx + dy * dy;
-      if (dim == 3) {
-        double dz = z[pa] - z[pb];
-        r2 += dz * dz;
-      }
-      double v = exp(-r2 * inv2s2);
-      if (i == j) v += shift;
-      A[(long long)i * nbk + j] = v;
     }
   }
 }
@@ -141,39 +143,54 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
 // ---- tile machinery (one CTA = one block) -------------------------------------------
 template <class T>
 struct Tiles {
-  T* As;  // [KC][S]
-  T* Bs;  // [KC][S]
+  T* As;  // [2][KC][S] (double buffered)
+  T* Bs;  // [2][KC][S]
   T* C;   // [TB][S] staging tile
   T* M;   // [TB][S] current diagonal inverse
 };
 
-// Stage a KC x TB chunk of an operand into dst[m][r] (r = output row/col index).
-// src element (r, m) at src[(row0 + r) * ld + col0 + m] if !trans, else
-// src[(row0 + m) * ld + col0 + r]. Out-of-range entries read as zero.
+// A KC x TB chunk of an operand, element (r, m) at src[(row0 + r) * ld + col0 + m] if
+// !trans, else src[(row0 + m) * ld + col0 + r]; out-of-range entries are zero. Fetched
+// into registers (issued early, so the loads overlap the previous chunk's arithmetic),
+// then written to shared memory as dst[m][r].
 template <class T>
-__device__ void stage(T* dst, const T* src, long long ld, int row0, int col0, int nr, int nm, bool trans) {
-  constexpr int S = SP<T>::S;
-  for (int e = threadIdx.x; e < KC * TB; e += NTH) {
-    int r, m;
-    if (!trans) {
-      m = e % KC;
-      r = e / KC;
-    } else {
-      r = e % TB;
-      m = e / TB;
+struct Chunk {
+  static constexpr int KC = KCOf<T>::v;
+  static constexpr int PER = KC * TB / NTH;
+  T v[PER];
+  __device__ __forceinline__ void fetch(const T* src, long long ld, int row0, int col0, int nr, int nm, bool trans) {
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      int e = threadIdx.x + q * NTH, r, m;
+      if (!trans) {
+        m = e % KC;
+        r = e / KC;
+      } else {
+        r = e % TB;
+        m = e / TB;
+      }
+      v[q] = (r < nr && m < nm) ? (trans ? src[(long long)(row0 + m) * ld + col0 + r]
+                                          : src[(long long)(row0 + r) * ld + col0 + m])
+                                : T(0);
     }
-    T v = T(0);
-    if (r < nr && m < nm) v = trans ? src[(long long)(row0 + m) * ld + col0 + r] : src[(long long)(row0 + r) * ld + col0 + m];
-    dst[m * S + r] = v;
   }
-}
+  __device__ __forceinline__ void store(T* dst, bool trans) const {
+    constexpr int S = SP<T>::S;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      int e = threadIdx.x + q * NTH;
+      int r = trans ? e % TB : e / KC, m = trans ? e / TB : e % KC;
+      dst[m * S + r] = v[q];
+    }
+  }
+};
 
 // acc[4][4] -= sum_m As[m][r] Bs[m][c] over the staged chunk
 template <class T>
 __device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4], int ty, int tx) {
   constexpr int S = SP<T>::S;
 #pragma unroll
-  for (int m = 0; m < KC; m++) {
+  for (int m = 0; m < KCOf<T>::v; m++) {
     T a[4], b[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -193,20 +210,32 @@ __device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4],
 template <class T>
 __device__ void tile_update(Tiles<T>& t, T acc[4][4], const T* P, long long ldp, int pr, int pc, int nr, bool ta,
                             const T* Q, long long ldq, int qr, int qc, int ncol, bool tb, int nm) {
+  constexpr int KC = KCOf<T>::v;
+  constexpr int S = SP<T>::S;
   int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-  for (int m0 = 0; m0 < nm; m0 += KC) {
+  const int nchunk = (nm + KC - 1) / KC;
+  Chunk<T> ca, cb;
+  auto fetch = [&](int m0) {
     int mm = min(KC, nm - m0);
-    __syncthreads();
     if (!ta)
-      stage<T>(t.As, P, ldp, pr, pc + m0, nr, mm, false);
+      ca.fetch(P, ldp, pr, pc + m0, nr, mm, false);
     else
-      stage<T>(t.As, P, ldp, pr + m0, pc, nr, mm, true);
+      ca.fetch(P, ldp, pr + m0, pc, nr, mm, true);
     if (!tb)
-      stage<T>(t.Bs, Q, ldq, qr, qc + m0, ncol, mm, false);
+      cb.fetch(Q, ldq, qr, qc + m0, ncol, mm, false);
     else
-      stage<T>(t.Bs, Q, ldq, qr + m0, qc, ncol, mm, true);
+      cb.fetch(Q, ldq, qr + m0, qc, ncol, mm, true);
+  };
+  __syncthreads();  // the previous user of the staging buffers is done
+  if (nchunk > 0) fetch(0);
+  for (int c = 0; c < nchunk; c++) {
+    T* As = t.As + (c & 1) * KC * S;
+    T* Bs = t.Bs + (c & 1) * KC * S;
+    ca.store(As, ta);
+    cb.store(Bs, tb);
     __syncthreads();
-    mma_chunk<T>(t.As, t.Bs, acc, ty, tx);
+    if (c + 1 < nchunk) fetch((c + 1) * KC);  // in flight during this chunk's arithmetic
+    mma_chunk<T>(As, Bs, acc, ty, tx);
   }
 }
 
@@ -349,10 +378,11 @@ __global__ void __launch_bounds__(NTH) k_chol_sc(int nblk, const int* __restrict
   if (b >= nblk || (only && !only[b])) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int S = SP<T>::S;
+  constexpr int KC = KCOf<T>::v;
   Tiles<T> t;
   t.As = (T*)smem_raw;
-  t.Bs = t.As + KC * S;
-  t.C = t.Bs + KC * S;
+  t.Bs = t.As + 2 * KC * S;
+  t.C = t.Bs + 2 * KC * S;
   t.M = t.C + TB * S;
   T* Minv_all = nullptr;  // diagonal inverses live in Xw after X (see xoff layout)
   int c = blk_cell[b];
@@ -407,9 +437,13 @@ __global__ void __launch_bounds__(NTH) k_chol_sc(int nblk, const int* __restrict
     // that it factors A = K / (2 pi sigma^2): L_A = L_K sqrt(1 / (2 pi sigma^2))
     T* Lp = Lpack + loff[c];
     const T sc = (T)out_scale;
+    // the diagonal is stored as its reciprocal: the substitutions then multiply
     for (int i = 0; i < nb; i++) {
       long long o = (long long)i * (i + 1) / 2;
-      for (int j = threadIdx.x; j <= i; j += NTH) Lp[o + j] = A[(long long)i * nb + j] * sc;
+      for (int j = threadIdx.x; j <= i; j += NTH) {
+        T v = A[(long long)i * nb + j] * sc;
+        Lp[o + j] = j == i ? T(1) / v : v;
+      }
     }
     if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
     return;
@@ -550,18 +584,34 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     if (w == 0) {
       T ri = lane < np ? y[p0 + lane] : T(0);
       for (int j = 0; j < np; j++) {
-        if (lane == j) ri = ri / tri[j][j];
+        if (lane == j) ri = ri * tri[j][j];  // reciprocal diagonal
         T yj = __shfl_sync(0xffffffffu, ri, j);
         if (lane > j) ri = fma(-tri[lane][j], yj, ri);
       }
       if (lane < np) y[p0 + lane] = ri;
     }
     __syncthreads();
-    const T yl = lane < np ? y[p0 + lane] : T(0);
-    for (int i = p0 + np + w; i < nb; i += nw) {
-      T v = lane < np ? L[(long long)i * (i + 1) / 2 + p0 + lane] * yl : T(0);
-      v = warp_sum(v);
-      if (lane == 0) y[i] -= v;
+    // rows below the panel: y[i] -= L[i][p0 .. p0+np) . y[p0 ..]. Four lanes per row, each
+    // with 8 contiguous entries, so 8 rows per warp pass and 2 shuffle levels: on GB300's
+    // narrow FP64 pipe a full warp reduction per row would cost 5x the row's FMAs.
+    {
+      const int sub = lane & 3, rw = lane >> 2;
+      T ys[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) ys[q] = (sub * 8 + q < np) ? y[p0 + sub * 8 + q] : T(0);
+      for (int i0 = p0 + np + 8 * w; i0 < nb; i0 += 8 * nw) {
+        const long long i = i0 + rw;
+        T acc = T(0);
+        if (i < nb) {
+          const T* Li = L + i * (i + 1) / 2 + p0 + sub * 8;
+#pragma unroll
+          for (int q = 0; q < 8; q++)
+            if (sub * 8 + q < np) acc = fma(Li[q], ys[q], acc);
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (sub == 0 && i < nb) y[i] -= acc;
+      }
     }
     __syncthreads();
   }
@@ -579,7 +629,7 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     if (w == 0) {  // x_i = (y_i - sum_{j > i} L22[j][i] x_j) / L22[i][i], i = np-1 .. 0
       T xi = lane < np ? y2[p0 + lane] : T(0);
       for (int j = np - 1; j >= 0; j--) {
-        if (lane == j) xi = xi / tri[j][j];
+        if (lane == j) xi = xi * tri[j][j];  // reciprocal diagonal
         T xj = __shfl_sync(0xffffffffu, xi, j);
         if (lane < j) xi = fma(-tri[j][lane], xj, xi);
       }
@@ -602,7 +652,7 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
 
 template <class T>
 size_t chol_smem() {
-  return sizeof(T) * (2 * KC * SP<T>::S + 2 * TB * SP<T>::S);
+  return sizeof(T) * (4 * KCOf<T>::v * SP<T>::S + 2 * TB * SP<T>::S);
 }
 
 }  // namespace
