@@ -46,7 +46,7 @@ enum {
 /* Initial guess of a solve. */
 enum {
   PRBF_GUESS_ZERO = 0,    /* zero initial guess, as the reference (no KSPSetInitialGuessNonzero) */
-  PRBF_GUESS_LEARNED = 1  /* per-cell MLP guess (requires prbf_guess_load) */
+  PRBF_GUESS_LEARNED = 1  /* per-cell MLP guess (weights from prbf_guess_set_weights) */
 };
 
 /* Flags of prbf_matvec_dev. */
@@ -86,6 +86,10 @@ typedef struct {
   double t_solve_ms;        /* Krylov / refinement iterations */
   double t_total_ms;        /* whole call incl. host<->device copies */
   long long pairs_per_matvec;
+  int guess_used;           /* 1 if the learned guess was kept (0: zero guess or dropped) */
+  double guess_rel_resid;   /* ||f - A g0||_2 / ||f||_2 of the learned guess (mixed) or its
+                               preconditioned residual relative to ||B f|| (plain); 1 = zero */
+  double t_guess_ms;        /* learned-guess inference */
 } prbf_stats;
 
 typedef struct prbf_ctx prbf_ctx;

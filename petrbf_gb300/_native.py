@@ -29,7 +29,8 @@ class Stats(ctypes.Structure):
                 ("rnorm", ctypes.c_double), ("true_rel_resid", ctypes.c_double),
                 ("t_sort_ms", ctypes.c_double), ("t_setup_ms", ctypes.c_double),
                 ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double),
-                ("pairs_per_matvec", ctypes.c_longlong)]
+                ("pairs_per_matvec", ctypes.c_longlong), ("guess_used", ctypes.c_int),
+                ("guess_rel_resid", ctypes.c_double), ("t_guess_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -68,6 +69,19 @@ SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    # learned initial guess (include/petrbf_gb300_learned.h)
+    "prbf_mlp_param_count": (ctypes.c_longlong, []),
+    "prbf_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_void_p)]),
+    "prbf_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "prbf_mlp_get_weights": (ctypes.c_int, [ctypes.c_void_p, _F]),
+    "prbf_mlp_set_weights": (ctypes.c_int, [ctypes.c_void_p, _F]),
+    "prbf_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _F, _F]),
+    "prbf_mlp_loss_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _F, _F, _F, _F, _F]),
+    "prbf_mlp_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _F, _F, _F, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_float, ctypes.c_ulonglong, _F]),
+    "prbf_guess_patches": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _D, _D, _D, _D, _F, _F, _F, _F, _I]),
+    "prbf_guess_set_weights": (ctypes.c_int, [ctypes.c_void_p, _F]),
+    "prbf_guess_eval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _D, _D, _D, _D]),
     "prbf_RBFInterpolation": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _F, _F, _F,
                                              _F, ctypes.c_int, _F, _F, _F, _F, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int]),

@@ -24,6 +24,7 @@ Grid make_grid(int dim, const double* bbox6, double sigma, int nsigma_box, int s
                int sigma_trunc);
 
 struct SolveState;  // solve.cu
+struct Mlp;         // mlp.h (learned initial guess)
 
 struct Ctx {
   prbf_params p{};
@@ -38,6 +39,7 @@ struct Ctx {
   bool mv_ready = false;
   DevBuf<double> vin, vout, vtmp;  // padded vectors of the matvec seam
   SolveState* solve = nullptr;  // owned; released by ~Ctx (solve.cu)
+  Mlp* guess = nullptr;         // owned; learned-guess network (prbf_guess_set_weights)
   ~Ctx();
 
   void check_device_error(const char* what);

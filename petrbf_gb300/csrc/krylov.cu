@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(KT) k_update_norm(const KState* __restrict__ s
 
 __device__ int converged_default(KState* s, int n, double rnorm) {
   // KSPConvergedDefault: rnorm0 at iteration 0, ttol = max(rtol rnorm0, abstol)
-  if (n == 0) {
+  if (n == 0 && !s->fixed_ref) {
     s->rnorm0 = rnorm;
     s->ttol = fmax(s->rtol * rnorm, s->abstol);
   }
@@ -323,26 +323,49 @@ void Krylov::build_graph(const Operator& op, cudaStream_t s) {
 }
 
 KResult Krylov::solve(const Operator& op, const double* b, double* x, bool zero_x, double rtol, double abstol, double dtol,
-                      int maxit, bool use_graph, cudaStream_t s) {
+                      int maxit, bool use_graph, cudaStream_t s, double rnorm_ref, bool guard) {
   KState h0{};
   h0.rtol = rtol;
   h0.abstol = abstol;
   h0.dtol = dtol;
   h0.maxit = maxit;
   h0.hist_cap = hist_cap;
+  if (rnorm_ref > 0) {
+    h0.fixed_ref = 1;
+    h0.rnorm0 = rnorm_ref;
+    h0.ttol = std::max(rtol * rnorm_ref, abstol);
+  }
   PRBF_CUDA(cudaMemcpyAsync(st.get(), &h0, sizeof(KState), cudaMemcpyHostToDevice, s));
   if (use_graph && graph_op != &op) build_graph(op, s);
   bool xzero = zero_x;
   KState hs{};
+  KResult r;
+  r.guess_used = !zero_x;
   for (int cycle = 0;; cycle++) {
     // v0 = B (b - A x); with a zero guess the product A x is skipped (as KSPInitialResidual)
-    if (!xzero) op.apply_A(x, t.get(), nullptr, s);
-    k_residual<<<nblk, KT, 0, s>>>(n, b, t.get(), t.get(), xzero ? 1 : 0);
-    op.apply_B(t.get(), w.get(), nullptr, s);
-    k_norm2_part<<<nblk, KT, 0, s>>>(w.get(), n, chunk, part2.get());
-    k_cycle_init<<<1, 32, 0, s>>>(st.get(), part2.get(), nblk, grs.get(), m, hist);
-    k_first_vector<<<nblk, KT, 0, s>>>(st.get(), w.get(), V.get(), vcur.get(), n);
-    PRBF_CHECK_LAUNCH();
+    auto prologue = [&]() {
+      if (!xzero) op.apply_A(x, t.get(), nullptr, s);
+      k_residual<<<nblk, KT, 0, s>>>(n, b, t.get(), t.get(), xzero ? 1 : 0);
+      op.apply_B(t.get(), w.get(), nullptr, s);
+      k_norm2_part<<<nblk, KT, 0, s>>>(w.get(), n, chunk, part2.get());
+      k_cycle_init<<<1, 32, 0, s>>>(st.get(), part2.get(), nblk, grs.get(), m, hist);
+      k_first_vector<<<nblk, KT, 0, s>>>(st.get(), w.get(), V.get(), vcur.get(), n);
+      PRBF_CHECK_LAUNCH();
+    };
+    prologue();
+    if (cycle == 0 && !zero_x && (guard || rnorm_ref > 0)) {
+      PRBF_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+      PRBF_CUDA(cudaStreamSynchronize(s));
+      r.guess_beta = hs.res;
+      if (guard && rnorm_ref > 0 && !(hs.res <= rnorm_ref)) {
+        // the guess is worse than starting from zero: drop it
+        PRBF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+        PRBF_CUDA(cudaMemcpyAsync(st.get(), &h0, sizeof(KState), cudaMemcpyHostToDevice, s));
+        xzero = true;
+        r.guess_used = false;
+        prologue();
+      }
+    }
     if (use_graph) {
       PRBF_CUDA(cudaGraphLaunch(exec, s));
     } else {
@@ -357,7 +380,6 @@ KResult Krylov::solve(const Operator& op, const double* b, double* x, bool zero_
     if (hs.done) break;
     if (cycle > maxit + 1) break;  // cannot happen: each cycle advances its or stops
   }
-  KResult r;
   r.its = hs.its;
   r.reason = hs.reason;
   r.rnorm0 = hs.beta0;

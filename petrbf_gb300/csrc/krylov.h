@@ -17,11 +17,14 @@ struct KState {
   double res;    // residual estimate |grs[k]|
   double scale;  // 1 / norm of the vector being normalised
   double beta0;  // first preconditioned residual norm
+  int fixed_ref; // rnorm0 / ttol given by the caller (not taken from the first residual)
 };
 
 struct KResult {
   int its = 0, reason = 0;
   double rnorm0 = 0, rnorm = 0;
+  bool guess_used = false;
+  double guess_beta = 0;  // first preconditioned residual of the given x
 };
 
 // y = A x and z = B r on cell-sorted vectors; kernels return immediately when *skip != 0
@@ -49,8 +52,11 @@ struct Krylov {
   ~Krylov();
   void init(int n, int m, cudaStream_t s);
   void reset_graph();
+  // rnorm_ref > 0: converge relative to rnorm_ref (e.g. ||B b|| when x starts from a
+  // guess) instead of the first residual; guard: if the first residual of a nonzero x is
+  // above rnorm_ref, x is reset to zero (the guess is dropped). guess_used reports which.
   KResult solve(const Operator& op, const double* b, double* x, bool zero_x, double rtol, double abstol, double dtol,
-                int maxit, bool use_graph, cudaStream_t s);
+                int maxit, bool use_graph, cudaStream_t s, double rnorm_ref = 0.0, bool guard = false);
 
  private:
   void iteration(const Operator& op, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond);

@@ -366,7 +366,7 @@ __device__ __forceinline__ void tile_range(int t, int n1, int nb, int kc1, int& 
 
 // One CTA per block: Cholesky, centre columns of the inverse, S_c.
 template <class T>
-__global__ void __launch_bounds__(NTH) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
+__global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
                                                  const long long* __restrict__ boff, const int* __restrict__ cs,
                                                  const long long* __restrict__ koff, T* __restrict__ K,
                                                  const long long* __restrict__ xoff, T* __restrict__ Xw,

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "krylov.h"
+#include "mlp.h"
 #include "rasm.h"
 
 namespace prbf {
@@ -58,6 +59,8 @@ struct SolveState {
 Ctx::~Ctx() {
   delete solve;
   solve = nullptr;
+  delete guess;
+  guess = nullptr;
   ctx_stream_release(*this);
 }
 
@@ -113,6 +116,9 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   }
   S.kry.graph_op = nullptr;  // operators are rebuilt per call
 
+  const bool use_guess = p.guess == PRBF_GUESS_LEARNED;
+  if (use_guess && (dim != 2 || !c.guess || !c.guess->ready))
+    throw Error(PRBF_ERR_STATE, "learned guess requested without installed weights (2D only)");
   prbf_stats st{};
   st.ncell = S.pts.g.ncell;
   st.max_block = S.rasm.max_nb;
@@ -126,14 +132,30 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
     PRBF_CUDA(cudaMemsetAsync(S.x.get(), 0, sizeof(double) * ld, c.stream));
     PRBF_CUDA(cudaStreamSynchronize(c.stream));
     const double ts0 = now_ms();
+    if (use_guess) {
+      // x0 from the network, in the solver's cell order (its inputs are the sorted points)
+      guess_compute(c, *c.guess, n, S.pts.x.get(), S.pts.y.get(), S.b.get(), S.x.get());
+      st.t_guess_ms += now_ms() - ts0;
+    }
     KResult kr;
     int outer = 0, inner_its = 0;
     if (!mixed) {
-      kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), true, p.rtol, p.abstol, p.dtol, p.max_it, true, c.stream);
+      double ref = 0.0;
+      if (use_guess) {
+        // converge relative to the zero-guess residual ||B b||, whatever the guess
+        S.op64.apply_B(S.b.get(), S.tmp.get(), nullptr, c.stream);
+        ref = norm2_host(S.tmp.get(), n, c.ws, c.stream);
+      }
+      kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), !use_guess, p.rtol, p.abstol, p.dtol, p.max_it, true, c.stream,
+                       ref, use_guess);
       inner_its = kr.its;
+      if (use_guess) {
+        st.guess_used = kr.guess_used ? 1 : 0;
+        st.guess_rel_resid = ref > 0 ? kr.guess_beta / ref : 1.0;
+      }
     } else {
       const double bnorm = norm2_host(S.b.get(), n, c.ws, c.stream);
-      bool xzero = true;
+      bool xzero = !use_guess;
       kr.reason = 0;
       for (outer = 0; outer < 50; outer++) {
         // r = b - A x in FP64
@@ -147,6 +169,16 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
           axpy_dev(n, -1.0, S.tmp.get(), S.r.get(), c.stream);  // r = b - Ax
         }
         double rn = norm2_host(S.r.get(), n, c.ws, c.stream);
+        if (outer == 0 && use_guess) {
+          st.guess_rel_resid = bnorm > 0 ? rn / bnorm : 1.0;
+          st.guess_used = rn <= bnorm ? 1 : 0;
+          if (!st.guess_used) {  // worse than zero: drop the guess
+            PRBF_CUDA(cudaMemsetAsync(S.x.get(), 0, sizeof(double) * ld, c.stream));
+            PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+            xzero = true;
+            rn = bnorm;
+          }
+        }
         if (outer == 0) kr.rnorm0 = rn;
         kr.rnorm = rn;
         if (!(rn == rn)) {
@@ -219,7 +251,6 @@ int prbf_interpolate(prbf_ctx* ctx, int n, const double* x, const double* y, con
     if (n <= 0 || n > (1 << 30)) throw Error(PRBF_ERR_ARG, "point count must be in [1, 2^30]");
     if (!x || !y || (c.p.dim == 3 && !z) || !f || !g_out || nrhs <= 0)
       throw Error(PRBF_ERR_ARG, "null array or nrhs <= 0");
-    if (c.p.guess == PRBF_GUESS_LEARNED) throw Error(PRBF_ERR_STATE, "no learned-guess model loaded");
     interpolate(c, n, x, y, z, f, nrhs, g_out, stats);
     return PRBF_OK;
   } catch (const Error& e) {

@@ -12,7 +12,7 @@ def _declared():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             src = open(os.path.join(ROOT, "include", f)).read()
-            names += re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\**(prbf_\w+)\s*\(", src, re.M)
+            names += re.findall(r"^\s*(?:[\w*]+\s+)+\**(prbf_\w+)\s*\(", src, re.M)
     return sorted(set(names))
 
 
