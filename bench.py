@@ -319,25 +319,37 @@ def run_ours(args, rank, world):
 
 
 def solve_section(p, dev, rank):
-    """Time-to-1e-13 of the full interpolation (cell list, RASM set-up, Krylov), plain FP64
-    (the reference's algorithm) and mixed precision, with the off-grid interpolation error."""
+    """Time-to-1e-13 of the full interpolation (cell list, RASM set-up, Krylov): plain FP64
+    (the reference's algorithm), mixed precision, and both with the learned initial guess
+    (petrbf_gb300/data/guess_mlp.npz), each with the off-grid interpolation error."""
+    from petrbf_gb300 import learned as L
     from petrbf_gb300.api import Context
     out = {}
-    for prec in ("fp64", "mixed"):
+    have_model = os.path.exists(L.MODEL_PATH)
+    variants = [("fp64", "zero"), ("mixed", "zero")]
+    if have_model:
+        variants += [("mixed", "learned"), ("fp64", "learned")]
+    for prec, guess in variants:
         with Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
-                     precision=prec, device=dev) as c:
+                     precision=prec, guess=guess, device=dev) as c:
+            if guess == "learned":
+                L.install(c)
             t0 = time.perf_counter()
             g, st = c.interpolate(p.x, p.y, None, p.f)
             wall = time.perf_counter() - t0
             err = offgrid_error(c, p, g)
         dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
-        out[prec] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s,
-                     "its": st.its, "outer_its": st.outer_its, "reason": st.reason,
-                     "true_rel_resid": st.true_rel_resid, "log10_err_offgrid": err,
-                     "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms,
-                     "t_solve_ms": st.t_solve_ms, "max_block": st.max_block,
-                     "blocks_shifted": st.nblocks_fallback}
+        key = prec if guess == "zero" else prec + "+learned"
+        out[key] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s,
+                    "its": st.its, "outer_its": st.outer_its, "reason": st.reason,
+                    "true_rel_resid": st.true_rel_resid, "log10_err_offgrid": err,
+                    "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms,
+                    "t_solve_ms": st.t_solve_ms, "t_guess_ms": st.t_guess_ms,
+                    "guess_used": st.guess_used, "guess_rel_resid": st.guess_rel_resid,
+                    "max_block": st.max_block, "blocks_shifted": st.nblocks_fallback}
     out["mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed"]["time_s"]
+    if have_model:
+        out["learned_mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed+learned"]["time_s"]
     out["metric"] = "pts/s to 1e-13 residual"
     return out
 

@@ -49,6 +49,14 @@ enum {
   PRBF_GUESS_LEARNED = 1  /* per-cell MLP guess (weights from prbf_guess_set_weights) */
 };
 
+/* Schwarz preconditioner type (PETSc -pc_asm_type; the reference leaves PCASM's default,
+ * restrict, in place and reads further options through KSPSetFromOptions at
+ * 2d/rbf_interpolation.cxx:211, 3d/rbf_interpolation.cxx:227). */
+enum {
+  PRBF_PC_RASM = 0,  /* restricted: each block's solution is kept on its centre cell only */
+  PRBF_PC_ASM = 1    /* basic: every block's whole solution is added back (symmetric B) */
+};
+
 /* Flags of prbf_matvec_dev. */
 enum {
   PRBF_ORDER_CALLER = 0, /* vectors in the order the points were given */
@@ -70,6 +78,7 @@ typedef struct {
   int precision;     /* PRBF_PREC_* */
   int guess;         /* PRBF_GUESS_* */
   int device;        /* CUDA device ordinal (default 0) */
+  int pc_type;       /* PRBF_PC_* (default PRBF_PC_RASM) */
 } prbf_params;
 
 typedef struct {
@@ -135,9 +144,10 @@ int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
 
 /* RASM preconditioner of the points given to prbf_matvec_setup: the reference's P shell
  * (MATOP_GET_SUBMATRICES = mysubmat, 2d/matmult.cxx:53-104) applied as PCASM with the
- * restricted prolongation of 2d/rbf_interpolation.cxx:213-229. precision PRBF_PREC_FP64
- * factorises the blocks in FP64, PRBF_PREC_MIXED in FP32. prbf_pc_apply computes z = B r
- * (host vectors, caller order). */
+ * restricted prolongation of 2d/rbf_interpolation.cxx:213-229 (or, with the context's
+ * pc_type = PRBF_PC_ASM, the basic one). precision PRBF_PREC_FP64 factorises the blocks in
+ * FP64, PRBF_PREC_MIXED in FP32. prbf_pc_apply computes z = B r (host vectors, caller
+ * order). */
 int prbf_pc_setup(prbf_ctx* ctx, int precision);
 int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
 

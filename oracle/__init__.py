@@ -50,12 +50,14 @@ def lib():
         _lib.orc_rasm_create.restype = ctypes.c_void_p
         _lib.orc_rasm_apply.argtypes = [ctypes.c_void_p, _D, _D]
         _lib.orc_rasm_destroy.argtypes = [ctypes.c_void_p]
+        _lib.orc_rasm_set_type.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib.orc_gmres.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, _D, _D, _D, _I,
                                    ctypes.c_void_p, _D, _D, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I, _I, _D]
         _lib.orc_rbf_interpolation.argtypes = [
             ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int,
-            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I, _I]
+            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I, _I,
+            ctypes.c_int]
         _lib.orc_vorticity_evaluation.argtypes = [
             ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_int, _D, _D, _D, _D,
             ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
@@ -172,9 +174,9 @@ def block(g, idx, xs, ys, zs):
 
 
 class Rasm:
-    """Restricted additive Schwarz with dense LU blocks (test oracle)."""
+    """Restricted (or, with basic=True, basic) additive Schwarz with dense LU blocks."""
 
-    def __init__(self, g, xs, ys, zs, cs):
+    def __init__(self, g, xs, ys, zs, cs, basic=False):
         self.g = g
         self.keep = (_f64(xs), _f64(ys), _f64(zs), cs)
         st = ctypes.c_int(0)
@@ -182,6 +184,7 @@ class Rasm:
                                        _d(self.keep[1]), _d(self.keep[2]), _i(cs),
                                        ctypes.byref(st))
         self.status = st.value
+        lib().orc_rasm_set_type(self.h, 1 if basic else 0)
 
     def apply(self, r):
         r = _f64(r)
@@ -213,8 +216,9 @@ def gmres(g, xs, ys, zs, cs, rasm, b, x0=None, rtol=1e-13, abstol=1e-50, dtol=1e
 
 
 def rbf_interpolation(x, y, z, f, sigma, nsigma_box, sigma_buffer, sigma_trunc, rtol=1e-13,
-                      restart=30, max_it=1000):
-    """Weights g with A g = f, in the caller's order (2d/rbf_interpolation.cxx:25-310)."""
+                      restart=30, max_it=1000, pc="rasm"):
+    """Weights g with A g = f, in the caller's order (2d/rbf_interpolation.cxx:25-310);
+    pc "asm" selects basic additive Schwarz (-pc_asm_type basic)."""
     x, y, z, f = _f64(x), _f64(y), _f64(z), _f64(f)
     n = x.shape[0]
     gout = np.zeros(n, np.float64)
@@ -223,7 +227,8 @@ def rbf_interpolation(x, y, z, f, sigma, nsigma_box, sigma_buffer, sigma_trunc, 
     _check(lib().orc_rbf_interpolation(3 if z is not None else 2, n, _d(x), _d(y), _d(z),
                                        _d(f), sigma, nsigma_box, sigma_buffer, sigma_trunc,
                                        rtol, restart, max_it, _d(gout), ctypes.byref(its),
-                                       ctypes.byref(reason)), "rbf_interpolation")
+                                       ctypes.byref(reason), 1 if pc == "asm" else 0),
+           "rbf_interpolation")
     return gout, its.value, reason.value
 
 

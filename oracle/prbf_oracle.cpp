@@ -194,6 +194,7 @@ struct Rasm {
   std::vector<long long> aoff;        // factor offsets (nb*nb each)
   std::vector<double> lu;             // LU factors (row-major)
   std::vector<int> piv;               // pivot rows, per block (offset = off)
+  int basic = 0;                      // PETSc -pc_asm_type basic instead of restrict
 };
 
 // Dense LU with partial pivoting (row interchanges), the algorithm PETSc's
@@ -430,10 +431,38 @@ void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y
   return R;
 }
 
+int orc_rasm_set_type(void* h, int basic) {
+  if (!h) return ERR_ARG;
+  ((Rasm*)h)->basic = basic ? 1 : 0;
+  return OK;
+}
+
+// Basic additive Schwarz (PCASM type basic, selectable through the reference's
+// KSPSetFromOptions, 2d/rbf_interpolation.cxx:211): out = sum_c R_c^T A_c^-1 R_c r over the
+// same subdomains; the block solutions are added in cell order (deterministic).
+static void asm_basic_apply(const Rasm* R, const double* r, double* out) {
+  std::vector<double> sol(R->off[R->ncell]);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int c = 0; c < R->ncell; c++) {
+    long long nb = R->off[c + 1] - R->off[c];
+    if (!nb) continue;
+    double* buf = sol.data() + R->off[c];
+    const int* id = R->idx.data() + R->off[c];
+    for (long long i = 0; i < nb; i++) buf[i] = r[id[i]];
+    lu_solve((int)nb, R->lu.data() + R->aoff[c], R->piv.data() + R->off[c], buf);
+  }
+  for (int i = 0; i < R->n; i++) out[i] = 0.0;
+  for (long long k = 0; k < R->off[R->ncell]; k++) out[R->idx[k]] += sol[k];
+}
+
 // Restricted additive Schwarz apply: subdomain = buffer set ("is"), prolongation only
 // onto the centre points ("is_local" = first n_c entries), 2d/rbf_interpolation.cxx:213-229.
 int orc_rasm_apply(void* h, const double* r, double* out) {
   Rasm* R = (Rasm*)h;
+  if (R->basic) {
+    asm_basic_apply(R, r, out);
+    return OK;
+  }
 #pragma omp parallel
   {
     std::vector<double> buf;
@@ -574,7 +603,7 @@ int orc_gmres(const orc_grid* g, int n, const double* x, const double* y, const 
 int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, const double* z,
                           const double* f, double sigma, int nsigma_box, int sigma_buffer,
                           int sigma_trunc, double rtol, int restart, int max_it, double* g_out,
-                          int* its, int* reason) {
+                          int* its, int* reason, int pc_basic) {
   if (n <= 0) return ERR_ARG;
   double b[6] = {x[0], x[0], y[0], y[0], dim == 3 ? z[0] : 0, dim == 3 ? z[0] : 0};
   for (int i = 0; i < n; i++) {
@@ -607,6 +636,7 @@ int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, cons
     orc_rasm_destroy(R);
     return st;
   }
+  orc_rasm_set_type(R, pc_basic);
   orc_gmres(&g, n, xs.data(), ys.data(), zp, cs.data(), R, fs.data(), nullptr, rtol, 1e-50,
             1e5, restart, max_it, gs.data(), its, reason, nullptr);
   orc_rasm_destroy(R);

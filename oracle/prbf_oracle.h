@@ -62,6 +62,7 @@ int orc_block(const orc_grid* g, int nb, const int* idx, const double* x,
 void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y,
                       const double* z, const int* cs, int* status);
 int orc_rasm_apply(void* h, const double* r, double* out);
+int orc_rasm_set_type(void* h, int basic);  /* 1: basic additive Schwarz (-pc_asm_type basic) */
 void orc_rasm_destroy(void* h);
 
 int orc_gmres(const orc_grid* g, int n, const double* x, const double* y,
@@ -73,7 +74,7 @@ int orc_rbf_interpolation(int dim, int n, const double* x, const double* y,
                           const double* z, const double* f, double sigma,
                           int nsigma_box, int sigma_buffer, int sigma_trunc,
                           double rtol, int restart, int max_it, double* g_out,
-                          int* its, int* reason);
+                          int* its, int* reason, int pc_basic);
 int orc_vorticity_evaluation(int dim, int nt, const double* xt, const double* yt,
                              const double* zt, int ns, const double* xs,
                              const double* ys, const double* zs, const double* gs,

@@ -28,7 +28,7 @@ class Context:
 
     def __init__(self, dim=2, sigma=0.025, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
                  rtol=1e-13, abstol=1e-50, dtol=1e5, restart=30, max_it=1000, precision="fp64",
-                 guess="zero", device=0):
+                 guess="zero", device=0, pc="rasm"):
         L = N.lib()
         p = N.Params()
         L.prbf_params_default(ctypes.byref(p))
@@ -38,6 +38,7 @@ class Context:
         p.restart, p.max_it, p.device = int(restart), int(max_it), int(device)
         p.precision = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
         p.guess = {"zero": N.GUESS_ZERO, "learned": N.GUESS_LEARNED}[guess]
+        p.pc_type = {"rasm": N.PC_RASM, "asm": N.PC_ASM}[pc]
         self.params = p
         self.dim = p.dim
         h = ctypes.c_void_p()
@@ -135,8 +136,12 @@ class Context:
         fr = np.ascontiguousarray(f.T if f.ndim == 2 else f)
         g = np.empty_like(fr)
         st = Stats()
-        self._check(N.lib().prbf_interpolate(self.h, n, _ptr(x), _ptr(y), _ptr(z), _ptr(fr), nrhs,
-                                              _ptr(g), ctypes.byref(st)))
+        code = N.lib().prbf_interpolate(self.h, n, _ptr(x), _ptr(y), _ptr(z), _ptr(fr), nrhs, _ptr(g),
+                                        ctypes.byref(st))
+        if code:
+            err = PrbfError(code, N.lib().prbf_last_error(self.h).decode())
+            err.stats = st  # iterations, residuals and times up to the failure
+            raise err
         return (g.T.copy() if f.ndim == 2 else g), st
 
     def evaluate(self, xt, yt, zt, xs, ys, zs, gs):

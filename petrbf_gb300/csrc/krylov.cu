@@ -312,8 +312,10 @@ void Krylov::build_graph(const Operator& op, cudaStream_t s) {
   try {
     iteration(op, s, cond, 1);
   } catch (...) {
-    cudaGraph_t dummy;
+    cudaGraph_t dummy = nullptr;
     cudaStreamEndCapture(s, &dummy);
+    cudaGetLastError();
+    graph_op = nullptr;
     throw;
   }
   cudaGraph_t captured;
@@ -336,7 +338,6 @@ KResult Krylov::solve(const Operator& op, const double* b, double* x, bool zero_
     h0.ttol = std::max(rtol * rnorm_ref, abstol);
   }
   PRBF_CUDA(cudaMemcpyAsync(st.get(), &h0, sizeof(KState), cudaMemcpyHostToDevice, s));
-  if (use_graph && graph_op != &op) build_graph(op, s);
   bool xzero = zero_x;
   KState hs{};
   KResult r;
@@ -366,6 +367,9 @@ KResult Krylov::solve(const Operator& op, const double* b, double* x, bool zero_
         prologue();
       }
     }
+    // capture after the first eager prologue, so launch-configuration errors of the
+    // operators surface outside the capture
+    if (use_graph && graph_op != &op) build_graph(op, s);
     if (use_graph) {
       PRBF_CUDA(cudaGraphLaunch(exec, s));
     } else {

@@ -553,13 +553,15 @@ __global__ void __launch_bounds__(128) k_apply(int ncell, const long long* __res
 // Forward substitution over the whole block (32-row panels: warp 0 solves the diagonal
 // triangle from shared memory, all warps update the rows below with coalesced row
 // segments), then the back substitution with L22^T only, since the centre unknowns are
-// the last n_c: x2 = L22^-T y2.
+// the last n_c: x2 = L22^-T y2. With full set (basic Schwarz) the back substitution runs
+// over the whole block and every entry is added into out (zeroed beforehand): points lie
+// in several blocks, so the adds are atomic.
 template <class T>
 __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* __restrict__ boff,
                                                    const int* __restrict__ cs, const int* __restrict__ idx,
                                                    const long long* __restrict__ loff, const T* __restrict__ Lpack,
                                                    const double* __restrict__ r, double* __restrict__ out,
-                                                   const int* __restrict__ skip) {
+                                                   const int* __restrict__ skip, int full) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tri[32][33];
@@ -615,15 +617,16 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     }
     __syncthreads();
   }
-  // backward on the centre block: L22^T x2 = y2, panels from the bottom
-  T* y2 = y + n1;
-  for (int pe = nc; pe > 0; pe -= 32) {
+  // backward on the trailing block (rows b0 ..): L22^T x2 = y2, panels from the bottom
+  const int b0 = full ? 0 : n1, nback = nb - b0;
+  T* y2 = y + b0;
+  for (int pe = nback; pe > 0; pe -= 32) {
     const int p0 = max(0, pe - 32), np = pe - p0;
     // tri[i][j] = L22[p0 + i][p0 + j], j <= i
     for (int e = tid; e < 32 * 32; e += blockDim.x) {
       int i = e >> 5, j = e & 31;
-      long long row = n1 + p0 + i;
-      tri[i][j] = (i < np && j <= i) ? L[row * (row + 1) / 2 + n1 + p0 + j] : T(0);
+      long long row = b0 + p0 + i;
+      tri[i][j] = (i < np && j <= i) ? L[row * (row + 1) / 2 + b0 + p0 + j] : T(0);
     }
     __syncthreads();
     if (w == 0) {  // x_i = (y_i - sum_{j > i} L22[j][i] x_j) / L22[i][i], i = np-1 .. 0
@@ -640,14 +643,24 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     for (int k = tid; k < p0; k += blockDim.x) {
       T acc = T(0);
       for (int j = 0; j < np; j++) {
-        long long row = n1 + p0 + j;
-        acc = fma(L[row * (row + 1) / 2 + n1 + k], y2[p0 + j], acc);
+        long long row = b0 + p0 + j;
+        acc = fma(L[row * (row + 1) / 2 + b0 + k], y2[p0 + j], acc);
       }
       y2[k] -= acc;
     }
     __syncthreads();
   }
-  for (int i = tid; i < nc; i += blockDim.x) out[cs[c] + i] = (double)y2[i];
+  if (full) {
+    for (int j = tid; j < nb; j += blockDim.x) atomicAdd(&out[id[j < n1 ? nc + j : j - n1]], (double)y[j]);
+  } else {
+    for (int i = tid; i < nc; i += blockDim.x) out[cs[c] + i] = (double)y2[i];
+  }
+}
+
+__global__ void k_zero_unless(long long n, double* __restrict__ v, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[i] = 0.0;
 }
 
 template <class T>
@@ -658,7 +671,7 @@ size_t chol_smem() {
 }  // namespace
 
 void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsigned* err, cudaStream_t s,
-                double ws_budget_bytes) {
+                double ws_budget_bytes, bool factor, bool basic) {
   (void)err;
   const Grid& g = P.g;
   R.fp32 = fp32;
@@ -697,14 +710,19 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
   size_t esz = fp32 ? sizeof(float) : sizeof(double);
   // FP64 form keeps the packed Cholesky factors (backward-stable triangular solves at
   // every apply); the FP32 form keeps S_c (one GEMV per apply)
-  R.factor = !fp32;
+  R.basic = basic;
+  R.n = P.n;
+  R.factor = !fp32 || factor || basic;
   if (R.factor) {
     std::vector<long long> hl(g.ncell + 1);
     hl[0] = 0;
     for (int c = 0; c < g.ncell; c++) hl[c + 1] = hl[c] + (long long)hcnt[c] * (hcnt[c] + 1) / 2;
     R.loff.reserve(g.ncell + 1);
     PRBF_CUDA(cudaMemcpyAsync(R.loff.get(), hl.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
-    R.L64.reserve(std::max<long long>(hl[g.ncell], 1));
+    if (fp32)
+      R.L32.reserve(std::max<long long>(hl[g.ncell], 1));
+    else
+      R.L64.reserve(std::max<long long>(hl[g.ncell], 1));
     PRBF_CUDA(cudaStreamSynchronize(s));
   } else {
     R.S32.reserve(std::max<long long>(hso[g.ncell], 1));
@@ -735,7 +753,7 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
       long long n1 = nbk - nc;
       long long ntile = (n1 + TB - 1) / TB + (nc + TB - 1) / TB;
       long long nct = (nc + TB - 1) / TB;
-      long long ke = nbk * nbk, xe = fp32 ? nbk * nct * TB + ntile * TB * TB : 1;
+      long long ke = nbk * nbk, xe = R.factor ? 1 : nbk * nct * TB + ntile * TB * TB;
       if (!bc.empty() && (double)(hk.back() + ke + hx.back() + xe) * esz > ws_budget_bytes) break;
       bc.push_back(c);
       hk.push_back(hk.back() + ke);
@@ -762,9 +780,14 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
         k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
                                              P.y.get(), zp, g.dim, inv2s2, shift, (float*)Kw, only);
         PRBF_CHECK_LAUNCH();
-        k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
-                                                     (float*)Xw, R.soff.get(), R.S32.get(), out_scale, dbad,
-                                                     only, 0, nullptr, nullptr);
+        if (R.factor)
+          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
+                                                       (float*)Xw, R.soff.get(), nullptr, std::sqrt(1.0 / out_scale),
+                                                       dbad, only, 1, R.loff.get(), R.L32.get());
+        else
+          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
+                                                       (float*)Xw, R.soff.get(), R.S32.get(), out_scale, dbad,
+                                                       only, 0, nullptr, nullptr);
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
                                               P.y.get(), zp, g.dim, inv2s2, shift, (double*)Kw, only);
@@ -791,9 +814,17 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
 void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s, const int* skip) {
   if (R.nblocks == 0) return;
   size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
-  if (R.factor)
+  if (R.basic) {
+    k_zero_unless<<<4 * 152, 256, 0, s>>>(R.n, out, skip);
+    PRBF_CHECK_LAUNCH();
+  }
+  const int full = R.basic ? 1 : 0;
+  if (R.factor && !R.fp32)
     k_apply_tri<double><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L64.get(), r,
-                                                 out, skip);
+                                                 out, skip, full);
+  else if (R.factor)
+    k_apply_tri<float><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L32.get(), r,
+                                                out, skip, full);
   else
     k_apply<float><<<R.ncell, 128, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.soff.get(), R.S32.get(), r, out,
                                             skip);
@@ -801,14 +832,16 @@ void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, 
 }
 
 void rasm_set_apply_smem(const RasmPlan& R) {
-  size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
-  if (sm > 48 * 1024) {
-    if (sm > 200 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
-    if (R.factor)
-      PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    else
-      PRBF_CUDA(cudaFuncSetAttribute(k_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  }
+  // dynamic: the block's right-hand side; static: k_apply_tri's 32 x 33 triangle tile
+  size_t sm = (size_t)std::max(R.max_nb, 1) * (R.fp32 ? sizeof(float) : sizeof(double));
+  size_t st = R.factor ? (R.fp32 ? sizeof(float) : sizeof(double)) * 32 * 33 : 0;
+  if (sm + st > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
+  if (R.factor && !R.fp32)
+    PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  else if (R.factor)
+    PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  else
+    PRBF_CUDA(cudaFuncSetAttribute(k_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
 }
 
 }  // namespace prbf

@@ -6,6 +6,8 @@ namespace prbf {
 
 struct RasmPlan {
   bool fp32 = false;
+  bool basic = false;         // basic Schwarz (whole block solutions added) instead of restricted
+  int n = 0;                  // points
   int ncell = 0, nblocks = 0;
   int max_nb = 0, max_nc = 0;
   int nfallback = 0;          // blocks that needed a diagonal-shift retry
@@ -14,17 +16,23 @@ struct RasmPlan {
   DevBuf<long long> soff;     // S_c offsets per cell (n_c * n_b each)
   bool factor = false;        // apply by triangular solves with the kept factor (FP64 form)
   DevBuf<long long> loff;     // packed-factor offsets per cell (n_b (n_b + 1) / 2 each)
-  DevBuf<double> L64;         // packed Cholesky factors (FP64 form), rows in block order
-  DevBuf<float> S32;          // S_c (FP32 form)
+  DevBuf<double> L64;         // packed Cholesky factors (FP64 factor form), rows in block order
+  DevBuf<float> L32;          // packed Cholesky factors (FP32 factor form)
+  DevBuf<float> S32;          // S_c (FP32 inverse-rows form)
 };
 
 // Buffer lists, blocks, factorisations and S_c for every non-empty cell of P.
 // ws_budget_bytes bounds the per-batch workspace (blocks are processed in batches).
+// factor: keep the packed factors and apply by triangular solves (always for FP64 and for
+// basic Schwarz; for restricted FP32 the alternative is S_c, one GEMV per apply).
+// basic: PETSc's -pc_asm_type basic, z = sum_c R_c^T A_c^-1 R_c r (symmetric); otherwise
+// the restricted form, z[centre(c)] = (A_c^-1 R_c r)[centre].
 void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsigned* err, cudaStream_t s,
-                double ws_budget_bytes);
+                double ws_budget_bytes, bool factor = false, bool basic = false);
 // Sets the dynamic shared memory limit of the apply kernel for this plan.
 void rasm_set_apply_smem(const RasmPlan& R);
-// out[centre(c)] = S_c r[buffer(c)] for every cell (sorted order, n entries).
+// Restricted: out[centre(c)] = (A_c^-1 r[buffer(c)])[centre] for every cell; basic:
+// out = sum_c R_c^T A_c^-1 R_c r (sorted order, n entries).
 void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s,
                 const int* skip = nullptr);
 
