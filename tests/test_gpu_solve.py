@@ -156,6 +156,85 @@ def test_solve_3d_small_matches_oracle():
     assert _rel(g, go) <= RTOL_WEIGHTS
 
 
+def _lattice3d_problem(m, seed):
+    x, y, z, h = W.lattice_3d(m, jitter=0.25, seed=seed)
+    return x, y, z, (h / 0.8, 2, 6, 16)  # cell 2 sigma, 2-sigma overlap, cutoff 7 sigma
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 5e-3)])
+def test_basic_asm_apply_matches_oracle_3d(precision, tol):
+    x, y, z, prm = _lattice3d_problem(12, 2)
+    g = O.grid_for(x, y, z, *prm)
+    perm, cs = O.cell_sort(g, x, y, z)
+    R = O.Rasm(g, x[perm], y[perm], z[perm], cs, basic=True)
+    r = np.random.default_rng(5).standard_normal(len(x))
+    ref = np.empty(len(x))
+    ref[perm] = R.apply(r[perm])
+    with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="asm") as c:
+        c.matvec_setup(x, y, z)
+        c.pc_setup(precision)
+        out = c.pc_apply(r)
+    # FP64: Cholesky vs pivoted LU of the same blocks, and atomic adds in any order
+    assert _rel(out, ref) < tol
+
+
+def test_basic_asm_solve_3d_matches_oracle():
+    # same Krylov path as the oracle's PETSc restatement: identical iteration counts
+    x, y, z, prm = _lattice3d_problem(12, 2)
+    wx = W.vortex_ring(x, y, z)[0]
+    for rtol in (1e-12, 1e-16):
+        go, its_o, reason_o = O.rbf_interpolation(x, y, z, wx, *prm, rtol=rtol, max_it=400, pc="asm")
+        with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="asm", rtol=rtol,
+                     max_it=400) as c:
+            g, st = c.interpolate(x, y, z, wx)
+        assert reason_o == 2 and st.reason == 2
+        assert abs(st.its - its_o) <= 1
+        assert _rel(g, go) <= RTOL_WEIGHTS
+
+
+def test_restricted_schwarz_stalls_on_jittered_3d_where_basic_converges():
+    x, y, z, prm = _lattice3d_problem(24, 12345)
+    wx = W.vortex_ring(x, y, z)[0]
+    with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, rtol=1e-12, max_it=150) as c:
+        with pytest.raises(PrbfError):
+            c.interpolate(x, y, z, wx)
+    with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, rtol=1e-12, max_it=150,
+                 pc="asm") as c:
+        _, st = c.interpolate(x, y, z, wx)
+    assert st.reason == 2 and st.true_rel_resid < 1e-11
+
+
+def test_mixed_3d_vortex_ring_components_match_fp64_oracle():
+    # the 3D mixed form at small size: FP32 matvec and FP32 block Cholesky inside FP64
+    # refinement to a true residual of 1e-12, three right-hand sides, each against the
+    # oracle's FP64 solve; omega_z of a ring about the z axis is identically zero
+    x, y, z, prm = _lattice3d_problem(16, 3)
+    F = np.stack(W.vortex_ring(x, y, z), axis=1)
+    with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="asm", precision="mixed",
+                 rtol=1e-12) as c:
+        g, st = c.interpolate(x, y, z, F)
+    assert st.reason in (2, 3) and st.true_rel_resid <= 1e-12
+    fnorm = np.linalg.norm(F)
+    for k in range(3):
+        go, _, reason = O.rbf_interpolation(x, y, z, F[:, k], *prm, rtol=1e-12, max_it=400, pc="asm")
+        if k == 2:
+            assert reason == 3 and np.abs(g[:, k]).max() == 0.0
+            continue
+        assert reason == 2
+        assert _rel(g[:, k], go) < 1e-9
+
+
+def test_large_subdomains_above_default_shared_memory():
+    # 73 x 73-point blocks: the apply kernel needs more than 48 KB of shared memory
+    x, y, h = W.lattice_2d(100)
+    f = W.lamb_oseen(x, y)
+    for pc in ("rasm", "asm"):
+        with Context(dim=2, sigma=h / 0.8, nsigma_box=16, sigma_buffer=58, sigma_trunc=32, rtol=1e-12, pc=pc) as c:
+            _, st = c.interpolate(x, y, None, f)
+        assert st.max_block * 8 + 32 * 33 * 8 > 48 * 1024
+        assert st.reason == 2 and st.true_rel_resid < 1e-10
+
+
 def test_rbfinterpolation_shim_matches_evaluate_then_solve():
     x, y, z, h = W.lattice_3d(10, jitter=0.0)
     sigma = h / 0.8
