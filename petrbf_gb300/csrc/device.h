@@ -95,8 +95,9 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
                     unsigned* err, Workspace& ws, cudaStream_t s);
 // w[i] = sum_{j in trunc(cell(i))} g[j] exp(-|t_i - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
 // for all sorted targets i; g must be a padded device vector of src.n (+2) entries.
+// w = A g for nv weight vectors at stride vstride (even; vectors padded as the sources)
 void gauss_sum_dev(const GaussPlan& plan, const PointsView& tgt, const PointsView& src,
                    const double* g, double* w, bool fp32, unsigned* err, cudaStream_t s,
-                   const int* skip = nullptr);
+                   const int* skip = nullptr, int nv = 1, long long vstride = 0);
 
 }  // namespace prbf

@@ -21,6 +21,9 @@
 // per pair, range reduction bits and the 2^-m scaling on the integer pipe); coordinates
 // relative to the cell centre, unscaled, so x_t - x_s rounds as in the reference. FP32
 // form: scaled FP32 coordinates relative to the cell centre and the SFU exp2.
+//
+// NV weight vectors (several right-hand sides of one point set, NV <= 4) are summed in
+// one pass: each pair's exponential is computed once and multiplies NV weights.
 #include <algorithm>
 #include <cmath>
 
@@ -43,9 +46,9 @@ constexpr int kTab = 1 << kTabBits;
 constexpr int kPoly = 5;  // degree-4 polynomial, coefficients T[j] L^i / i!
 __device__ double d_tab[kPoly][kTab];  // copied into shared memory by each CTA
 
-template <int DIM, bool F32>
+template <int DIM, bool F32, int NV>
 struct Cfg {
-  static constexpr int kComp = (F32 ? 2048 : (DIM == 3 ? 1536 : 2048));
+  static constexpr int kComp = (NV > 1 ? 1024 : (F32 ? 2048 : (DIM == 3 ? 1536 : 2048)));
   using T = typename std::conditional<F32, float, double>::type;
 };
 
@@ -58,15 +61,15 @@ struct Piece {
 constexpr size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
 // Dynamic shared memory carve-up of k_gauss (byte offsets, each 16-byte aligned).
-template <int DIM, bool F32>
+template <int DIM, bool F32, int NV>
 struct Layout {
-  using T = typename Cfg<DIM, F32>::T;
-  static constexpr int NA = DIM + 1;
+  using T = typename Cfg<DIM, F32, NV>::T;
+  static constexpr int NA = DIM + NV;
   static constexpr size_t raw = 0;
   static constexpr size_t comp = align16(raw + sizeof(double) * NA * kRawCap);
-  static constexpr size_t tgt = align16(comp + sizeof(T) * NA * Cfg<DIM, F32>::kComp);
+  static constexpr size_t tgt = align16(comp + sizeof(T) * NA * Cfg<DIM, F32, NV>::kComp);
   static constexpr size_t acc = align16(tgt + sizeof(T) * DIM * kTileT);
-  static constexpr size_t tab = align16(acc + sizeof(T) * kTileT);
+  static constexpr size_t tab = align16(acc + sizeof(T) * NV * kTileT);
   static constexpr size_t pieces = align16(tab + (F32 ? 0 : sizeof(double) * kPoly * kTab));
   static constexpr size_t bar = align16(pieces + sizeof(Piece) * kMaxPieces);
   static constexpr size_t total = bar + 16;
@@ -84,23 +87,23 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
-template <int DIM, bool F32>
+template <int DIM, bool F32, int NV>
 __global__ void __launch_bounds__(kThreads) k_gauss(
     Grid g, const int2* __restrict__ items, const double* __restrict__ tx, const double* __restrict__ ty,
     const double* __restrict__ tz, const int* __restrict__ cs_t, const double* __restrict__ sx,
     const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
-    const int* __restrict__ cs_s, double* __restrict__ w, double scale, double kexp, double norm,
-    unsigned* err, const int* __restrict__ skip) {
+    const int* __restrict__ cs_s, double* __restrict__ w, long long vstride, double scale, double kexp,
+    double norm, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  using C = Cfg<DIM, F32>;
+  using C = Cfg<DIM, F32, NV>;
   using T = typename C::T;
-  constexpr int NA = DIM + 1;  // staged arrays: coordinates + weight
+  constexpr int NA = DIM + NV;  // staged arrays: coordinates + weights
   extern __shared__ __align__(16) unsigned char smem[];
-  const Layout<DIM, F32> lay;
+  const Layout<DIM, F32, NV> lay;
   double* raw = (double*)(smem + lay.raw);      // NA x kRawCap (FP64, as stored in HBM)
   T* comp = (T*)(smem + lay.comp);              // NA x kComp (compacted truncation set)
   T* tgt = (T*)(smem + lay.tgt);                // DIM x kTileT
-  T* acc = (T*)(smem + lay.acc);                // kTileT
+  T* acc = (T*)(smem + lay.acc);                // NV x kTileT
   double* tab = (double*)(smem + lay.tab);      // kPoly x kTab (FP64 form only)
   Piece* pieces = (Piece*)(smem + lay.pieces);  // kMaxPieces
   uint64_t* bar = (uint64_t*)(smem + lay.bar);
@@ -131,7 +134,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
     tgt[t] = (T)((tx[t0 + t] - xc) * scale);
     tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
     if (DIM == 3) tgt[2 * kTileT + t] = (T)((tz[t0 + t] - zc) * scale);
-    acc[t] = T(0);
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v * kTileT + t] = T(0);
   }
   if (!F32)
     for (int i = tid; i < kPoly * kTab; i += kThreads) tab[i] = (&d_tab[0][0])[i];
@@ -151,19 +155,22 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   auto flush = [&]() {
     for (int gi = wid; gi < ngroups; gi += kWarps) {
       T tu[kGroup], tv[kGroup], tw[kGroup];
-      T a[kGroup];
+      T a[kGroup][NV];
 #pragma unroll
       for (int k = 0; k < kGroup; k++) {
         int t = min(gi * kGroup + k, nt - 1);
         tu[k] = tgt[t];
         tv[k] = tgt[kTileT + t];
         tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : T(0);
-        a[k] = T(0);
+#pragma unroll
+        for (int v = 0; v < NV; v++) a[k][v] = T(0);
       }
       for (int j = lane; j < ncomp; j += 32) {
         T su = comp[j], sv = comp[C::kComp + j];
         T sw = DIM == 3 ? comp[2 * C::kComp + j] : T(0);
-        T sgj = comp[(NA - 1) * C::kComp + j];
+        T sgj[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) sgj[v] = comp[(DIM + v) * C::kComp + j];
 #pragma unroll
         for (int k = 0; k < kGroup; k++) {
           T du = tu[k] - su, dv = tv[k] - sv;
@@ -174,7 +181,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             d2 = fma(dw, dw, d2);
           }
           if constexpr (F32) {
-            a[k] = fmaf(sgj, ex2_approx(-d2), a[k]);
+            const float e = ex2_approx(-d2);
+#pragma unroll
+            for (int v = 0; v < NV; v++) a[k][v] = fmaf(sgj[v], e, a[k][v]);
           } else {
             // d2 = |x_t - x_s|^2 (unscaled: the differences are exact as in the reference);
             // in units of L = ln2/kTab the exponent is kexp*d2, kexp = kTab/(2 sigma^2 ln2):
@@ -191,15 +200,19 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             q = fma(r, q, hi_sub(tab[2 * kTab + j8], m20));
             q = fma(r, q, hi_sub(tab[1 * kTab + j8], m20));
             q = fma(r, q, hi_sub(tab[j8], m20));
-            a[k] = fma(sgj, q, a[k]);
+#pragma unroll
+            for (int v = 0; v < NV; v++) a[k][v] = fma(sgj[v], q, a[k][v]);
           }
         }
       }
 #pragma unroll
       for (int k = 0; k < kGroup; k++) {
-        T s = warp_sum(a[k]);
         int t = gi * kGroup + k;
-        if (lane == 0 && t < nt) acc[t] += s;
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          T s = warp_sum(a[k][v]);
+          if (lane == 0 && t < nt) acc[v * kTileT + t] += s;
+        }
       }
     }
     ncomp = 0;
@@ -253,7 +266,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
           bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
           bulk_g2s(raw + kRawCap + dst, sy + s_al, len * 8u, bar);
           if (DIM == 3) bulk_g2s(raw + 2 * kRawCap + dst, sz + s_al, len * 8u, bar);
-          bulk_g2s(raw + (NA - 1) * kRawCap + dst, sg + s_al, len * 8u, bar);
+#pragma unroll
+          for (int v = 0; v < NV; v++) bulk_g2s(raw + (DIM + v) * kRawCap + dst, sg + v * vstride + s_al, len * 8u, bar);
         }
       }
     }
@@ -283,13 +297,14 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
       for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
         int e = e0 + tid;
         bool in = false;
-        double vx = 0, vy = 0, vz = 0, vg = 0;
+        double vx = 0, vy = 0, vz = 0;
+        int ro = 0;
         if (e < pc.count) {
-          int j = pc.gstart + e, ro = pc.raw_off + e;
+          int j = pc.gstart + e;
+          ro = pc.raw_off + e;
           vx = raw[ro];
           vy = raw[kRawCap + ro];
           if (DIM == 3) vz = raw[2 * kRawCap + ro];
-          vg = raw[(NA - 1) * kRawCap + ro];
           // centre cell unconditionally (2d/get_trunc.h:31-39), neighbours by the box test
           // fabs(xj - xc) < trunc_length && ... (2d/get_trunc.h:63; 3d/get_trunc.h:70-72)
           bool boxin = fabs(vx - xc) < L && fabs(vy - yc) < L;
@@ -311,7 +326,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
           comp[pos] = (T)((vx - xc) * scale);
           comp[C::kComp + pos] = (T)((vy - yc) * scale);
           if (DIM == 3) comp[2 * C::kComp + pos] = (T)((vz - zc) * scale);
-          comp[(NA - 1) * C::kComp + pos] = (T)vg;
+#pragma unroll
+          for (int v = 0; v < NV; v++) comp[(DIM + v) * C::kComp + pos] = (T)raw[(DIM + v) * kRawCap + ro];
         }
         ncomp += tot;
         __syncthreads();
@@ -320,7 +336,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   }
   flush();
   __syncthreads();
-  for (int t = tid; t < nt; t += kThreads) w[t0 + t] = (double)acc[t] * norm;
+  for (int t = tid; t < nt; t += kThreads)
+#pragma unroll
+    for (int v = 0; v < NV; v++) w[v * vstride + t0 + t] = (double)acc[v * kTileT + t] * norm;
 }
 
 // ---- work list and truncation-set sizes ----------------------------------------------
@@ -402,20 +420,21 @@ void upload_table(cudaStream_t s) {
   if (dev < 64) g_tab_ready[dev] = true;
 }
 
-template <int DIM, bool F32>
+template <int DIM, bool F32, int NV>
 size_t smem_bytes() {
-  return Layout<DIM, F32>::total;
+  return Layout<DIM, F32, NV>::total;
 }
 
-template <int DIM, bool F32>
+template <int DIM, bool F32, int NV>
 void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
-            unsigned* err, const int* skip, cudaStream_t st) {
-  size_t sm = smem_bytes<DIM, F32>();
+            long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
+  size_t sm = smem_bytes<DIM, F32, NV>();
+  static_assert(Layout<DIM, F32, NV>::total <= 227 * 1024, "k_gauss shared memory");
   static bool attr_set[64] = {false};
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
-    PRBF_CUDA(cudaFuncSetAttribute(k_gauss<DIM, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss<DIM, F32, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
   const double sigma = P.g.sigma;
@@ -425,9 +444,25 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   // to units of ln2/kTab inside the fused range reduction.
   const double scale = F32 ? std::sqrt(1.0 / (2.0 * sigma * sigma * std::log(2.0))) : 1.0;
   const double kexp = (double)kTab / (2.0 * sigma * sigma * std::log(2.0));
-  k_gauss<DIM, F32><<<P.nitems, kThreads, sm, st>>>(P.g, P.items.get(), t.x, t.y, t.z, t.cell_start,
-                                                    s.x, s.y, s.z, gv, s.cell_start, w, scale, kexp, norm, err, skip);
+  k_gauss<DIM, F32, NV><<<P.nitems, kThreads, sm, st>>>(P.g, P.items.get(), t.x, t.y, t.z, t.cell_start, s.x, s.y,
+                                                        s.z, gv, s.cell_start, w, vstride, scale, kexp, norm, err,
+                                                        skip);
   PRBF_CHECK_LAUNCH();
+}
+
+template <int DIM, bool F32>
+void launch_nv(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w, int nv,
+               long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
+  for (int v0 = 0; v0 < nv; v0 += 4) {
+    const double* g0 = gv + v0 * vstride;
+    double* w0 = w + v0 * vstride;
+    switch (std::min(4, nv - v0)) {
+      case 1: launch<DIM, F32, 1>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      case 2: launch<DIM, F32, 2>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      case 3: launch<DIM, F32, 3>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      default: launch<DIM, F32, 4>(P, t, s, g0, w0, vstride, err, skip, st); break;
+    }
+  }
 }
 
 }  // namespace
@@ -469,18 +504,21 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
 }
 
 void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv,
-                   double* w, bool fp32, unsigned* err, cudaStream_t st, const int* skip) {
-  if (P.nitems == 0) return;
+                   double* w, bool fp32, unsigned* err, cudaStream_t st, const int* skip, int nv,
+                   long long vstride) {
+  if (P.nitems == 0 || nv <= 0) return;
+  if (nv > 1 && (vstride % 2 || vstride < t.n || vstride < s.n))
+    throw Error(PRBF_ERR_ARG, "vector stride must be even and cover the points");
   if (P.g.dim == 2) {
     if (fp32)
-      launch<2, true>(P, t, s, gv, w, err, skip, st);
+      launch_nv<2, true>(P, t, s, gv, w, nv, vstride, err, skip, st);
     else
-      launch<2, false>(P, t, s, gv, w, err, skip, st);
+      launch_nv<2, false>(P, t, s, gv, w, nv, vstride, err, skip, st);
   } else {
     if (fp32)
-      launch<3, true>(P, t, s, gv, w, err, skip, st);
+      launch_nv<3, true>(P, t, s, gv, w, nv, vstride, err, skip, st);
     else
-      launch<3, false>(P, t, s, gv, w, err, skip, st);
+      launch_nv<3, false>(P, t, s, gv, w, nv, vstride, err, skip, st);
   }
 }
 

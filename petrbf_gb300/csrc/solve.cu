@@ -9,6 +9,7 @@
 // approximately by GMRES whose matvec and RASM blocks are FP32; FP64 is kept for the outer
 // residual matvec, the Arnoldi vectors and Hessenberg least squares, and the update. It
 // stops on the true residual ||f - A g||_2 <= rtol ||f||_2.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -22,17 +23,20 @@ namespace prbf {
 
 namespace {
 
+// A and B over nv right-hand sides stored at stride vstride
 struct GaussRasmOp : Operator {
   const GaussPlan* plan = nullptr;
   PointsView v{};
   const RasmPlan* rasm = nullptr;
   bool fp32 = false;
   unsigned* err = nullptr;
+  int nv = 1;
+  long long vstride = 0;
   void apply_A(const double* x, double* y, const int* skip, cudaStream_t s) const override {
-    gauss_sum_dev(*plan, v, v, x, y, fp32, err, s, skip);
+    gauss_sum_dev(*plan, v, v, x, y, fp32, err, s, skip, nv, vstride);
   }
   void apply_B(const double* r, double* z, const int* skip, cudaStream_t s) const override {
-    rasm_apply(*rasm, v.cell_start, r, z, s, skip);
+    for (int k = 0; k < nv; k++) rasm_apply(*rasm, v.cell_start, r + k * vstride, z + k * vstride, s, skip);
   }
 };
 
@@ -100,23 +104,30 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   c.check_device_error("RASM set-up");
   const double t_setup = now_ms();
 
+  // right-hand sides: segments of one vector at a 32-aligned stride, solved in lockstep
+  // (the matvec computes each pair's exponential once for all of them)
+  const int nv = nrhs;
+  const long long ldn = ((long long)n + 4 + 31) / 32 * 32;
+  const long long len_all = ldn * nv + 32;
   S.op64.plan = S.op32.plan = &S.plan;
   S.op64.v = S.op32.v = S.pts.view();
   S.op64.rasm = S.op32.rasm = &S.rasm;
   S.op64.err = S.op32.err = c.err.get();
   S.op64.fp32 = false;
   S.op32.fp32 = true;
-  const long long ld = (long long)n + 4;
-  S.b.reserve(ld);
-  S.x.reserve(ld);
-  S.r.reserve(ld);
-  S.d.reserve(ld);
-  S.tmp.reserve(ld);
-  for (auto* v : {&S.b, &S.x, &S.r, &S.d, &S.tmp}) PRBF_CUDA(cudaMemsetAsync(v->get(), 0, sizeof(double) * ld, c.stream));
-  if (S.kry.n != n || S.kry.m != p.restart) {
-    S.kry.reset_graph();
-    S.kry.init(n, p.restart, c.stream);
-  }
+  S.op64.nv = S.op32.nv = nv;
+  S.op64.vstride = S.op32.vstride = ldn;
+  S.b.reserve(len_all);
+  S.x.reserve(len_all);
+  S.r.reserve(len_all);
+  S.d.reserve(len_all);
+  S.tmp.reserve(len_all);
+  for (auto* v : {&S.b, &S.x, &S.r, &S.d, &S.tmp})
+    PRBF_CUDA(cudaMemsetAsync(v->get(), 0, sizeof(double) * len_all, c.stream));
+  std::vector<long long> offs(nv);
+  std::vector<int> lens(nv, n);
+  for (int v = 0; v < nv; v++) offs[v] = v * ldn;
+  if (!S.kry.same_layout(offs, lens, p.restart)) S.kry.init(offs, lens, len_all, p.restart, c.stream);
   S.kry.graph_op = nullptr;  // operators are rebuilt per call
 
   const bool use_guess = p.guess == PRBF_GUESS_LEARNED;
@@ -127,106 +138,153 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   st.max_block = S.rasm.max_nb;
   st.nblocks_fallback = S.rasm.nfallback;
   st.pairs_per_matvec = S.plan.pairs;
-  double t_solve = 0;
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    const double* fr = f + (size_t)rhs * n;
-    PRBF_CUDA(cudaMemcpyAsync(S.tmp.get(), fr, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
-    gather_dev(n, S.pts.perm.get(), S.tmp.get(), S.b.get(), c.stream);
-    PRBF_CUDA(cudaMemsetAsync(S.x.get(), 0, sizeof(double) * ld, c.stream));
-    PRBF_CUDA(cudaStreamSynchronize(c.stream));
-    const double ts0 = now_ms();
-    if (use_guess) {
-      // x0 from the network, in the solver's cell order (its inputs are the sorted points)
-      guess_compute(c, *c.guess, n, S.pts.x.get(), S.pts.y.get(), S.b.get(), S.x.get());
-      st.t_guess_ms += now_ms() - ts0;
-    }
-    KResult kr;
-    int outer = 0, inner_its = 0;
-    if (!mixed) {
-      double ref = 0.0;
-      if (use_guess) {
-        // converge relative to the zero-guess residual ||B b||, whatever the guess
-        S.op64.apply_B(S.b.get(), S.tmp.get(), nullptr, c.stream);
-        ref = norm2_host(S.tmp.get(), n, c.ws, c.stream);
-      }
-      kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), !use_guess, p.rtol, p.abstol, p.dtol, p.max_it, true, c.stream,
-                       ref, use_guess);
-      inner_its = kr.its;
-      if (use_guess) {
-        st.guess_used = kr.guess_used ? 1 : 0;
-        st.guess_rel_resid = ref > 0 ? kr.guess_beta / ref : 1.0;
-      }
-    } else {
-      const double bnorm = norm2_host(S.b.get(), n, c.ws, c.stream);
-      bool xzero = !use_guess;
-      kr.reason = 0;
-      for (outer = 0; outer < 50; outer++) {
-        // r = b - A x in FP64
-        if (xzero) {
-          PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
-        } else {
-          S.op64.apply_A(S.x.get(), S.r.get(), nullptr, c.stream);
-          axpy_dev(n, -1.0, S.b.get(), S.r.get(), c.stream);  // r = Ax - b
-          PRBF_CUDA(cudaMemcpyAsync(S.tmp.get(), S.r.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
-          PRBF_CUDA(cudaMemsetAsync(S.r.get(), 0, sizeof(double) * n, c.stream));
-          axpy_dev(n, -1.0, S.tmp.get(), S.r.get(), c.stream);  // r = b - Ax
-        }
-        double rn = norm2_host(S.r.get(), n, c.ws, c.stream);
-        if (outer == 0 && use_guess) {
-          st.guess_rel_resid = bnorm > 0 ? rn / bnorm : 1.0;
-          st.guess_used = rn <= bnorm ? 1 : 0;
-          if (!st.guess_used) {  // worse than zero: drop the guess
-            PRBF_CUDA(cudaMemsetAsync(S.x.get(), 0, sizeof(double) * ld, c.stream));
-            PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
-            xzero = true;
-            rn = bnorm;
-          }
-        }
-        if (outer == 0) kr.rnorm0 = rn;
-        kr.rnorm = rn;
-        if (!(rn == rn)) {
-          kr.reason = -9;
-          break;
-        }
-        if (rn <= p.rtol * bnorm || rn <= p.abstol) {
-          kr.reason = rn <= p.abstol ? 3 : 2;
-          break;
-        }
-        if (inner_its >= p.max_it) {
-          kr.reason = -3;
-          break;
-        }
-        PRBF_CUDA(cudaMemsetAsync(S.d.get(), 0, sizeof(double) * ld, c.stream));
-        int budget_its = std::min(p.max_it - inner_its, 4 * p.restart);
-        KResult in = S.kry.solve(S.op32, S.r.get(), S.d.get(), true, 1e-6, 0.0, 1e10, budget_its, true, c.stream);
-        inner_its += in.its;
-        axpy_dev(n, 1.0, S.d.get(), S.x.get(), c.stream);
-        xzero = false;
-        if (in.its == 0) {
-          kr.reason = -5;
-          break;
-        }
-      }
-      if (!kr.reason) kr.reason = -3;
-    }
-    PRBF_CUDA(cudaStreamSynchronize(c.stream));
-    t_solve += now_ms() - ts0;
-    c.check_device_error("solve");
-    // weights back in the caller's order (2d/rbf_interpolation.cxx:246-265)
-    scatter_dev(n, S.pts.perm.get(), S.x.get(), S.tmp.get(), c.stream);
-    PRBF_CUDA(cudaMemcpyAsync(g_out + (size_t)rhs * n, S.tmp.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
-    // true residual ||b - A x|| / ||b|| in FP64 (reported, not part of the solve)
-    S.op64.apply_A(S.x.get(), S.r.get(), nullptr, c.stream);
-    axpy_dev(n, -1.0, S.b.get(), S.r.get(), c.stream);
-    double rr = norm2_host(S.r.get(), n, c.ws, c.stream), bn = norm2_host(S.b.get(), n, c.ws, c.stream);
-    st.its += inner_its;
-    st.outer_its += outer;
-    st.reason = kr.reason;
-    st.rnorm0 = kr.rnorm0;
-    st.rnorm = kr.rnorm;
-    st.true_rel_resid = std::max(st.true_rel_resid, bn > 0 ? rr / bn : rr);
-    if (kr.reason < 0) break;
+  for (int v = 0; v < nv; v++) {
+    PRBF_CUDA(cudaMemcpyAsync(S.tmp.get(), f + (size_t)v * n, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+    gather_dev(n, S.pts.perm.get(), S.tmp.get(), S.b.get() + v * ldn, c.stream);
   }
+  PRBF_CUDA(cudaMemsetAsync(S.tmp.get(), 0, sizeof(double) * len_all, c.stream));
+  PRBF_CUDA(cudaStreamSynchronize(c.stream));
+  const double ts0 = now_ms();
+  if (use_guess) {
+    // x0 from the network, in the solver's cell order (its inputs are the sorted points)
+    for (int v = 0; v < nv; v++)
+      guess_compute(c, *c.guess, n, S.pts.x.get(), S.pts.y.get(), S.b.get() + v * ldn, S.x.get() + v * ldn);
+    PRBF_CUDA(cudaStreamSynchronize(c.stream));
+    st.t_guess_ms = now_ms() - ts0;
+  }
+  std::vector<int> reason(nv, 0), its(nv, 0), outer(nv, 0);
+  std::vector<double> rnorm0(nv, 0.0), rnorm(nv, 0.0);
+  if (!mixed) {
+    std::vector<double> ref(nv, 0.0);
+    if (use_guess) {
+      // converge relative to the zero-guess residual ||B b||, whatever the guess
+      S.op64.apply_B(S.b.get(), S.tmp.get(), nullptr, c.stream);
+      std::vector<double> q = seg_norm2_host(S.kry, S.tmp.get(), c.stream);
+      for (int v = 0; v < nv; v++) ref[v] = std::sqrt(q[v]);
+    }
+    std::vector<KResult> kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), !use_guess, p.rtol, p.abstol, p.dtol, p.max_it,
+                                          true, c.stream, use_guess ? ref.data() : nullptr, use_guess);
+    int used = 0;
+    double gres = 0;
+    for (int v = 0; v < nv; v++) {
+      its[v] = kr[v].its;
+      reason[v] = kr[v].reason;
+      rnorm0[v] = kr[v].rnorm0;
+      rnorm[v] = kr[v].rnorm;
+      used += kr[v].guess_used ? 1 : 0;
+      gres = std::max(gres, ref[v] > 0 ? kr[v].guess_beta / ref[v] : 1.0);
+    }
+    if (use_guess) {
+      st.guess_used = used == nv ? 1 : 0;
+      st.guess_rel_resid = gres;
+    }
+  } else {
+    std::vector<double> bnorm = seg_norm2_host(S.kry, S.b.get(), c.stream);
+    for (auto& q : bnorm) q = std::sqrt(q);
+    bool xzero = !use_guess;
+    int inner_max = 0;
+    const int nall = (int)(ldn * nv);
+    for (int it = 0; it < 50; it++) {
+      // r = b - A x in FP64 (all right-hand sides)
+      if (xzero) {
+        PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * nall, cudaMemcpyDeviceToDevice, c.stream));
+      } else {
+        S.op64.apply_A(S.x.get(), S.tmp.get(), nullptr, c.stream);
+        PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * nall, cudaMemcpyDeviceToDevice, c.stream));
+        axpy_dev(nall, -1.0, S.tmp.get(), S.r.get(), c.stream);
+      }
+      std::vector<double> rn = seg_norm2_host(S.kry, S.r.get(), c.stream);
+      for (auto& q : rn) q = std::sqrt(q);
+      if (it == 0 && use_guess) {
+        int used = 0;
+        double gres = 0;
+        for (int v = 0; v < nv; v++) {
+          gres = std::max(gres, bnorm[v] > 0 ? rn[v] / bnorm[v] : 1.0);
+          if (rn[v] <= bnorm[v]) {
+            used++;
+            continue;
+          }
+          // worse than zero: drop the guess of this right-hand side
+          PRBF_CUDA(cudaMemsetAsync(S.x.get() + v * ldn, 0, sizeof(double) * n, c.stream));
+          PRBF_CUDA(cudaMemcpyAsync(S.r.get() + v * ldn, S.b.get() + v * ldn, sizeof(double) * n,
+                                    cudaMemcpyDeviceToDevice, c.stream));
+          rn[v] = bnorm[v];
+        }
+        st.guess_used = used == nv ? 1 : 0;
+        st.guess_rel_resid = gres;
+      }
+      bool all = true;
+      for (int v = 0; v < nv; v++) {
+        if (it == 0) rnorm0[v] = rn[v];
+        if (reason[v]) {
+          // stopped earlier: keep it out of the inner solve (zero residual stops at once)
+          PRBF_CUDA(cudaMemsetAsync(S.r.get() + v * ldn, 0, sizeof(double) * n, c.stream));
+          continue;
+        }
+        rnorm[v] = rn[v];
+        if (!(rn[v] == rn[v])) {
+          reason[v] = -9;
+        } else if (rn[v] <= p.rtol * bnorm[v] || rn[v] <= p.abstol) {
+          reason[v] = rn[v] <= p.abstol ? 3 : 2;
+        } else if (inner_max >= p.max_it) {
+          reason[v] = -3;
+        } else {
+          outer[v]++;
+          all = false;
+          continue;
+        }
+        PRBF_CUDA(cudaMemsetAsync(S.r.get() + v * ldn, 0, sizeof(double) * n, c.stream));
+      }
+      if (all) break;
+      PRBF_CUDA(cudaMemsetAsync(S.d.get(), 0, sizeof(double) * len_all, c.stream));
+      int budget_its = std::min(p.max_it - inner_max, 4 * p.restart);
+      std::vector<KResult> in = S.kry.solve(S.op32, S.r.get(), S.d.get(), true, 1e-6, 0.0, 1e10, budget_its, true,
+                                            c.stream);
+      int step = 0;
+      bool progress = false;
+      for (int v = 0; v < nv; v++) {
+        if (reason[v]) continue;
+        its[v] += in[v].its;
+        step = std::max(step, in[v].its);
+        progress = progress || in[v].its > 0;
+      }
+      inner_max += step;
+      axpy_dev(nall, 1.0, S.d.get(), S.x.get(), c.stream);
+      xzero = false;
+      if (!progress) {
+        for (int v = 0; v < nv; v++)
+          if (!reason[v]) reason[v] = -5;
+        break;
+      }
+    }
+    for (int v = 0; v < nv; v++)
+      if (!reason[v]) reason[v] = -3;
+  }
+  PRBF_CUDA(cudaStreamSynchronize(c.stream));
+  const double t_solve = now_ms() - ts0;
+  c.check_device_error("solve");
+  // weights back in the caller's order (2d/rbf_interpolation.cxx:246-265)
+  for (int v = 0; v < nv; v++) {
+    scatter_dev(n, S.pts.perm.get(), S.x.get() + v * ldn, S.tmp.get(), c.stream);
+    PRBF_CUDA(cudaMemcpyAsync(g_out + (size_t)v * n, S.tmp.get(), sizeof(double) * n, cudaMemcpyDeviceToHost,
+                              c.stream));
+  }
+  // true residual ||b - A x|| / ||b|| in FP64 (reported, not part of the solve)
+  S.op64.apply_A(S.x.get(), S.r.get(), nullptr, c.stream);
+  axpy_dev((int)(ldn * nv), -1.0, S.b.get(), S.r.get(), c.stream);
+  std::vector<double> rr = seg_norm2_host(S.kry, S.r.get(), c.stream), bn = seg_norm2_host(S.kry, S.b.get(), c.stream);
+  // reason: the first failure if any, else 2 (rtol) unless every system stopped on atol
+  st.reason = 3;
+  for (int v = 0; v < nv; v++) {
+    double q = std::sqrt(rr[v]), bq = std::sqrt(bn[v]);
+    st.true_rel_resid = std::max(st.true_rel_resid, bq > 0 ? q / bq : q);
+    st.its += its[v];
+    st.outer_its += outer[v];
+    if (st.reason < 0) continue;
+    if (reason[v] < 0 || reason[v] == 2) st.reason = reason[v];
+  }
+  st.rnorm0 = rnorm0[nv - 1];
+  st.rnorm = rnorm[nv - 1];
   st.t_sort_ms = t_sorted - t_begin;
   st.t_setup_ms = t_setup - t_sorted;
   st.t_solve_ms = t_solve;

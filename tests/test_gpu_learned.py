@@ -59,7 +59,9 @@ def test_trained_guess_reduces_iterations_on_held_out_problem(precision):
         L.install(c)
         g1, st1 = c.interpolate(p.x, p.y, None, p.f)
     assert st0.reason == 2 and st1.reason == 2
-    assert st1.guess_used == 1 and st1.guess_rel_resid < 0.1
+    # guess_rel_resid: the guess's true residual relative to ||f|| (mixed), its
+    # preconditioned residual relative to ||B f|| (plain)
+    assert st1.guess_used == 1 and st1.guess_rel_resid < (0.1 if precision == "mixed" else 0.5)
     # the same final residual, reached in fewer Krylov (or refinement) iterations
     if precision == "fp64":
         assert st1.its < st0.its
