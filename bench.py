@@ -12,6 +12,8 @@ every step. The full solve to 1e-13 (plain FP64 and mixed precision) is timed on
 after the steps and reported under ``solve``.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--skip-solve]
+    python bench.py --workload vortex3d     # 3D mixed form, 128^3, three right-hand sides
+    python bench.py --workload batch2d      # 256 problems of uneven N in one batch
 """
 import argparse
 import json
@@ -40,6 +42,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-solve", action="store_true")
     ap.add_argument("--m", type=int, default=2000, help="lattice edge (N = m^2)")
+    ap.add_argument("--workload", default="matvec2d", choices=["matvec2d", "vortex3d", "batch2d"],
+                    help="matvec2d: the headline line; vortex3d / batch2d: the 3D mixed and batched forms")
+    ap.add_argument("--m3", type=int, default=128, help="3D lattice edge (vortex3d)")
+    ap.add_argument("--nprob", type=int, default=256, help="problems (batch2d)")
+    ap.add_argument("--batch-max-it", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -354,10 +361,77 @@ def solve_section(p, dev, rank):
     return out
 
 
+def run_vortex3d(args, rank):
+    """The 3D mixed-precision form: 128^3 jittered lattice, three vortex-ring right-hand
+    sides, FP32 matvec + FP32 block Cholesky inside FP64 refinement to 1e-12, against the
+    plain FP64 GPU solve of the same problem (the form the tests pin to the oracle)."""
+    from petrbf_gb300 import workloads as W
+    from petrbf_gb300.api import Context
+    p = W.config3(m=args.m3)
+    nb, sb, st_ = p.nsigma_box, p.sigma_buffer, p.sigma_trunc
+    out = {}
+    sols = {}
+    for prec in ("mixed", "fp64"):
+        with Context(dim=3, sigma=p.sigma, nsigma_box=nb, sigma_buffer=sb, sigma_trunc=st_, precision=prec,
+                     rtol=1e-12, pc="asm") as c:
+            t0 = time.perf_counter()
+            g, st = c.interpolate(p.x, p.y, p.z, p.f)
+            wall = time.perf_counter() - t0
+        sols[prec] = g
+        dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
+        out[prec] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s, "its": st.its,
+                     "outer_its": st.outer_its, "reason": st.reason, "true_rel_resid": st.true_rel_resid,
+                     "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms, "t_solve_ms": st.t_solve_ms,
+                     "max_block": st.max_block, "pairs_per_matvec": st.pairs_per_matvec}
+    gm, gd = sols["mixed"], sols["fp64"]
+    comp = {}
+    for k, name in enumerate(("omega_x", "omega_y", "omega_z")):
+        dn = float(np.linalg.norm(gd[:, k]))
+        diff = float(np.linalg.norm(gm[:, k] - gd[:, k]))
+        comp[name] = {"weights_rel_diff_vs_fp64": diff / dn if dn > 0 else None,
+                      "weights_abs_diff_vs_fp64": diff, "fp64_weights_norm": dn}
+    out["components"] = comp
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed"]["time_s"]
+    print(json.dumps({"metric": "pts/s to 1e-12, 3D mixed, 3 right-hand sides", "value": out["mixed"]["pts_per_s"],
+                      "unit": "pts/s", "higher_is_better": True, "dtype": "f32/f64", "data": "synthetic",
+                      "config": {"workload": p.name, "n_points": p.n, "nsigma_box": nb, "sigma_buffer": sb,
+                                 "sigma_trunc": st_, "pc": "asm (basic additive Schwarz)", "rhs": 3},
+                      "solve": out}), flush=True)
+
+
+def run_batch2d(args, rank):
+    """The batched form: 256 problems of uneven N solved together (FP64, basic Schwarz)."""
+    from petrbf_gb300 import workloads as W
+    from petrbf_gb300.api import batch_interpolate
+    probs = W.config4(nprob=args.nprob)
+    res = {}
+    for rep in range(2):  # second call: schedule from the autotuner's cache
+        t0 = time.perf_counter()
+        g, its, reason, st = batch_interpolate(probs, rtol=1e-13, pc="asm", max_it=args.batch_max_it)
+        wall = time.perf_counter() - t0
+        res[rep] = (st, wall, its, reason)
+    st, wall, its, reason = res[1]
+    dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_tune_ms + st.t_solve_ms) * 1e-3
+    print(json.dumps({"metric": "pts/s to 1e-13, batched 2D", "value": st.points / dev_s, "unit": "pts/s",
+                      "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "batched_2d_%d_problems" % args.nprob, "n_points": st.points,
+                                 "pc": "asm (basic additive Schwarz)"},
+                      "batch": dict(st.as_dict(), wall_s=wall, first_call_tune_ms=res[0][0].t_tune_ms,
+                                    its_median=float(np.median(its)), its_max=int(np.max(its)),
+                                    unconverged=int(np.sum(reason <= 0)),
+                                    matvec_gpairs_per_s_in_solve=None)}), flush=True)
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
-    if args.impl == "reference":
+    if args.workload == "vortex3d":
+        if rank == 0:
+            run_vortex3d(args, rank)
+    elif args.workload == "batch2d":
+        if rank == 0:
+            run_batch2d(args, rank)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world)

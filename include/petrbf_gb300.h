@@ -151,6 +151,43 @@ int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
 int prbf_pc_setup(prbf_ctx* ctx, int precision);
 int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
 
+/* ---- batches of independent problems (no reference counterpart: the reference solves
+ * one problem per call; this is the replica form for many small problems on one GPU) ---- */
+
+/* One problem of a batch; dimension, tolerances, restart, iteration limit and the Schwarz
+ * type come from the context's parameters (FP64, zero guess). */
+typedef struct {
+  int n;
+  const double *x, *y, *z;  /* caller-order coordinates (z null in 2D) */
+  const double* f;          /* right-hand side */
+  double sigma;
+  int nsigma_box, sigma_buffer, sigma_trunc;
+  double* g_out;            /* weights, caller order (n entries) */
+} prbf_problem;
+
+typedef struct {
+  int nprob;
+  int nconverged;           /* problems that met the tolerance */
+  int max_its, total_its;   /* GMRES iterations: slowest problem, sum over problems */
+  long long points;
+  long long pairs_per_matvec;
+  int ncell, nblocks, min_block, max_block, nblocks_fallback;
+  int tile, grid;           /* Gaussian-sum schedule chosen by the autotuner (grid 0: one
+                               CTA per item) */
+  double max_true_rel_resid;/* max over problems of ||f - A g||_2 / ||f||_2 */
+  double t_sort_ms;         /* uploads, cell lists, truncation and buffer sizes */
+  double t_setup_ms;        /* batched block factorisation */
+  double t_tune_ms;         /* autotuning (0 when the schedule came from the cache) */
+  double t_solve_ms;        /* lockstep GMRES */
+  double t_total_ms;
+} prbf_batch_stats;
+
+/* Solves every problem with GMRES + Schwarz blocks in one set of launches per iteration
+ * (rbf_interpolation per problem, 2d/rbf_interpolation.cxx:25-310); its_out / reason_out
+ * (nullable) receive each problem's iterations and KSPConvergedReason-style code. */
+int prbf_batch_interpolate(prbf_ctx* ctx, int nprob, const prbf_problem* probs, int* its_out, int* reason_out,
+                           prbf_batch_stats* stats);
+
 /* RBFInterpolation (3d/wrapper.cxx:20-105): FP32 in/out, evaluates the particles
  * (xp, yp, zp, gp) at the grid points first when xg[0] != xp[0], then solves on the
  * grid and writes the weights over wg. argc/argv are accepted and ignored. */

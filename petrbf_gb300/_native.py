@@ -36,6 +36,25 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Problem(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("f", ctypes.c_void_p), ("sigma", ctypes.c_double), ("nsigma_box", ctypes.c_int),
+                ("sigma_buffer", ctypes.c_int), ("sigma_trunc", ctypes.c_int), ("g_out", ctypes.c_void_p)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("nprob", ctypes.c_int), ("nconverged", ctypes.c_int), ("max_its", ctypes.c_int),
+                ("total_its", ctypes.c_int), ("points", ctypes.c_longlong),
+                ("pairs_per_matvec", ctypes.c_longlong), ("ncell", ctypes.c_int), ("nblocks", ctypes.c_int),
+                ("min_block", ctypes.c_int), ("max_block", ctypes.c_int), ("nblocks_fallback", ctypes.c_int),
+                ("tile", ctypes.c_int), ("grid", ctypes.c_int), ("max_true_rel_resid", ctypes.c_double),
+                ("t_sort_ms", ctypes.c_double), ("t_setup_ms", ctypes.c_double), ("t_tune_ms", ctypes.c_double),
+                ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # status codes (PRBF_*)
 OK, ERR_ARG, ERR_RANGE, ERR_CAPACITY, ERR_CUDA, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_NAN, \
     ERR_STATE, ERR_FACTOR, ERR_DIVERGED, ERR_TIMEOUT = range(12)
@@ -70,6 +89,8 @@ SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    "prbf_batch_interpolate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Problem), _I, _I,
+                                              ctypes.POINTER(BatchStats)]),
     # learned initial guess (include/petrbf_gb300_learned.h)
     "prbf_mlp_param_count": (ctypes.c_longlong, []),
     "prbf_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_void_p)]),

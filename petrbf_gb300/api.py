@@ -152,6 +152,35 @@ class Context:
         return w
 
 
+def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="asm", device=0):
+    """Solves many independent problems together. problems: sequence of dicts with keys x,
+    y, (z), f, sigma, nsigma_box, sigma_buffer, sigma_trunc. Returns (list of weight
+    arrays, iterations per problem, reason per problem, BatchStats)."""
+    keep, probs, outs = [], [], []
+    for q in problems:
+        arrs = [_f64(q[k]) for k in ("x", "y")] + [_f64(q.get("z")), _f64(q["f"])]
+        g = np.empty(arrs[0].shape[0], np.float64)
+        keep.append(arrs)
+        outs.append(g)
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        probs.append(N.Problem(arrs[0].shape[0], ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]), ptr(arrs[3]),
+                               float(q["sigma"]), int(q["nsigma_box"]), int(q["sigma_buffer"]),
+                               int(q["sigma_trunc"]), g.ctypes.data))
+    arr = (N.Problem * len(probs))(*probs)
+    its = np.zeros(len(probs), np.int32)
+    reason = np.zeros(len(probs), np.int32)
+    st = N.BatchStats()
+    with Context(dim=dim, rtol=rtol, restart=restart, max_it=max_it, pc=pc, device=device) as c:
+        code = N.lib().prbf_batch_interpolate(c.h, len(probs), arr, its.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                              reason.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                              ctypes.byref(st))
+        if code:
+            err = PrbfError(code, N.lib().prbf_last_error(c.h).decode())
+            err.stats = st
+            raise err
+    return outs, its, reason, st
+
+
 class GaussianOperator:
     """The truncated Gaussian operator of a point set (the reference's MatShell M)."""
 

@@ -41,12 +41,22 @@ struct Error : std::runtime_error {
 struct Grid {
   int dim;
   int nx, ny, nz, ncell;
+  int cbase;                // global index of the first cell (batches of grids; else 0)
   int nb_trunc, nb_buffer;
   double sigma;
   double xmin, ymin, zmin;  // particle minimum - epsf
   double box;               // nsigma_box*sigma + epsf
   double trunc_len;         // sigma_trunc*sigma/2 + epsf
   double buffer_len;        // sigma_buffer*sigma/2 + epsf
+};
+
+// Work of stopped systems in a batch: cell -> problem, and the problems' stop flags
+// (done[prob * stride], e.g. inside the Krylov per-system state); inactive when done is null.
+struct SegSkip {
+  const int* cprob = nullptr;
+  const int* done = nullptr;
+  int stride = 0;
+  __device__ bool cell_done(int c) const { return done && done[(long long)cprob[c] * stride]; }
 };
 
 __host__ __device__ inline int cell_of(const Grid& g, int ix, int iy, int iz) {

@@ -24,6 +24,8 @@ Grid make_grid(int dim, const double* bbox6, double sigma, int nsigma_box, int s
                int sigma_trunc);
 
 struct SolveState;  // solve.cu
+struct BatchState;  // batch.cu
+void batch_state_free(BatchState* b);
 struct Mlp;         // mlp.h (learned initial guess)
 
 struct Ctx {
@@ -40,6 +42,7 @@ struct Ctx {
   DevBuf<double> vin, vout, vtmp;  // padded vectors of the matvec seam
   SolveState* solve = nullptr;  // owned; released by ~Ctx (solve.cu)
   Mlp* guess = nullptr;         // owned; learned-guess network (prbf_guess_set_weights)
+  BatchState* batch = nullptr;  // owned; state of prbf_batch_interpolate
   ~Ctx();
 
   void check_device_error(const char* what);

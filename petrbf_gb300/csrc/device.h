@@ -86,8 +86,13 @@ struct GaussPlan {
   int max_tile = 0;
   long long pairs = 0;
   int max_trunc = 0;
+  int grid = 0;           // CTAs of a launch (0: one per item; fewer: persistent rounds)
+  bool batched = false;   // cells index a concatenation of grids (grids, cprob)
   DevBuf<int2> items;     // (cell, first target of the tile)
   DevBuf<int> trunc_cnt;  // truncation-set size per target cell
+  DevBuf<Grid> grids;     // batched: one grid per problem (with its first global cell)
+  DevBuf<int> cprob;      // batched: problem of each global cell
+  SegSkip seg;            // batched: skip the items of stopped problems (when seg.done set)
 };
 
 // Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc.

@@ -87,13 +87,32 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
-template <int DIM, bool F32, int NV>
+// Per-problem constants of the sum (from sigma): FP32 coordinate scale, FP64 exponent
+// factor, normalisation. The host computes the same expressions for single problems.
+struct SumConsts {
+  double scale, kexp, norm;
+};
+
+__host__ __device__ inline SumConsts sum_consts(double sigma, bool f32) {
+  const double ln2 = 0.6931471805599453;  // ln 2 rounded to double
+  SumConsts k;
+  k.scale = f32 ? sqrt(1.0 / (2.0 * sigma * sigma * ln2)) : 1.0;
+  k.kexp = (double)kTab / (2.0 * sigma * sigma * ln2);
+  k.norm = 1.0 / (2 * 3.141592653589793 * sigma * sigma);
+  return k;
+}
+
+// Items are processed in rounds of gridDim.x (snake order over the list, which a batched
+// plan sorts by decreasing cost): with one CTA per item this is the plain launch, with
+// fewer CTAs it is a persistent kernel. BATCH: the item's cell indexes a concatenation of
+// grids (cell -> problem -> Grid with its first global cell and sigma).
+template <int DIM, bool F32, int NV, bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_gauss(
-    Grid g, const int2* __restrict__ items, const double* __restrict__ tx, const double* __restrict__ ty,
-    const double* __restrict__ tz, const int* __restrict__ cs_t, const double* __restrict__ sx,
-    const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
-    const int* __restrict__ cs_s, double* __restrict__ w, long long vstride, double scale, double kexp,
-    double norm, unsigned* err, const int* __restrict__ skip) {
+    Grid g0, const Grid* __restrict__ grids, const int* __restrict__ cprob, const int2* __restrict__ items, int nitems,
+    const double* __restrict__ tx, const double* __restrict__ ty, const double* __restrict__ tz,
+    const int* __restrict__ cs_t, const double* __restrict__ sx, const double* __restrict__ sy,
+    const double* __restrict__ sz, const double* __restrict__ sg, const int* __restrict__ cs_s, double* __restrict__ w,
+    long long vstride, SumConsts k0, SegSkip seg, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
   using C = Cfg<DIM, F32, NV>;
   using T = typename C::T;
@@ -113,232 +132,249 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   __shared__ int s_abort;
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int2 item = items[blockIdx.x];
-  const int ic = item.x, t0 = item.y;
-  const int nt = min(kTileT, cs_t[ic + 1] - t0);
-  int ix, iy, iz;
-  cell_xyz(g, ic, ix, iy, iz);
-  const double xc = centre_coord(g.xmin, ix, g.box);
-  const double yc = centre_coord(g.ymin, iy, g.box);
-  const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
-  const double L = g.trunc_len;
-  const int c0 = cs_s[ic], c1 = cs_s[ic + 1];
-  const int nb = g.nb_trunc;
-  const int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
-  const int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
-  const int jz0 = DIM == 3 ? max(0, iz - nb) : 0, jz1 = DIM == 3 ? min(g.nz - 1, iz + nb) : 0;
-  const int ncolx = jx1 - jx0 + 1;
-  const int nranges = ncolx * (jz1 - jz0 + 1);
-
-  for (int t = tid; t < nt; t += kThreads) {
-    tgt[t] = (T)((tx[t0 + t] - xc) * scale);
-    tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
-    if (DIM == 3) tgt[2 * kTileT + t] = (T)((tz[t0 + t] - zc) * scale);
-#pragma unroll
-    for (int v = 0; v < NV; v++) acc[v * kTileT + t] = T(0);
-  }
   if (!F32)
     for (int i = tid; i < kPoly * kTab; i += kThreads) tab[i] = (&d_tab[0][0])[i];
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    s_cursor[0] = 0;  // range index
-    s_cursor[1] = -1; // position inside the range (-1: start of range)
-    s_abort = 0;
-  }
-  __syncthreads();
-
-  int ncomp = 0;
+  if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
-  const int ngroups = (nt + kGroup - 1) / kGroup;
+  const int G = gridDim.x;
 
-  // pair loop over comp[0, ncomp) for all targets of the tile
-  auto flush = [&]() {
-    for (int gi = wid; gi < ngroups; gi += kWarps) {
-      T tu[kGroup], tv[kGroup], tw[kGroup];
-      T a[kGroup][NV];
+  for (int round = 0; (long long)round * G < nitems; round++) {
+    const int it = (round & 1) ? round * G + (G - 1 - (int)blockIdx.x) : round * G + (int)blockIdx.x;
+    if (it >= nitems) continue;
+    const int2 item = items[it];
+    const int ic = item.x, t0 = item.y;
+    Grid g = g0;
+    SumConsts kc = k0;
+    if constexpr (BATCH) {
+      if (seg.cell_done(ic)) continue;  // a stopped problem (uniform over the CTA)
+      g = grids[cprob[ic]];
+      kc = sum_consts(g.sigma, F32);
+    }
+    const double scale = kc.scale, kexp = kc.kexp;
+    const int cb = g.cbase;
+    const int nt = min(kTileT, cs_t[ic + 1] - t0);
+    int ix, iy, iz;
+    cell_xyz(g, ic - cb, ix, iy, iz);
+    const double xc = centre_coord(g.xmin, ix, g.box);
+    const double yc = centre_coord(g.ymin, iy, g.box);
+    const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+    const double L = g.trunc_len;
+    const int c0 = cs_s[ic], c1 = cs_s[ic + 1];
+    const int nb = g.nb_trunc;
+    const int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+    const int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+    const int jz0 = DIM == 3 ? max(0, iz - nb) : 0, jz1 = DIM == 3 ? min(g.nz - 1, iz + nb) : 0;
+    const int ncolx = jx1 - jx0 + 1;
+    const int nranges = ncolx * (jz1 - jz0 + 1);
+
+    __syncthreads();  // the previous item's readers of tgt/acc/comp are done
+    for (int t = tid; t < nt; t += kThreads) {
+      tgt[t] = (T)((tx[t0 + t] - xc) * scale);
+      tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
+      if (DIM == 3) tgt[2 * kTileT + t] = (T)((tz[t0 + t] - zc) * scale);
 #pragma unroll
-      for (int k = 0; k < kGroup; k++) {
-        int t = min(gi * kGroup + k, nt - 1);
-        tu[k] = tgt[t];
-        tv[k] = tgt[kTileT + t];
-        tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : T(0);
-#pragma unroll
-        for (int v = 0; v < NV; v++) a[k][v] = T(0);
-      }
-      for (int j = lane; j < ncomp; j += 32) {
-        T su = comp[j], sv = comp[C::kComp + j];
-        T sw = DIM == 3 ? comp[2 * C::kComp + j] : T(0);
-        T sgj[NV];
-#pragma unroll
-        for (int v = 0; v < NV; v++) sgj[v] = comp[(DIM + v) * C::kComp + j];
+      for (int v = 0; v < NV; v++) acc[v * kTileT + t] = T(0);
+    }
+    if (tid == 0) {
+      s_cursor[0] = 0;  // range index
+      s_cursor[1] = -1; // position inside the range (-1: start of range)
+      s_abort = 0;
+    }
+    __syncthreads();
+
+    int ncomp = 0;
+    const int ngroups = (nt + kGroup - 1) / kGroup;
+
+    // pair loop over comp[0, ncomp) for all targets of the tile
+    auto flush = [&]() {
+      for (int gi = wid; gi < ngroups; gi += kWarps) {
+        T tu[kGroup], tv[kGroup], tw[kGroup];
+        T a[kGroup][NV];
 #pragma unroll
         for (int k = 0; k < kGroup; k++) {
-          T du = tu[k] - su, dv = tv[k] - sv;
-          T d2 = du * du;
-          d2 = fma(dv, dv, d2);
-          if (DIM == 3) {
-            T dw = tw[k] - sw;
-            d2 = fma(dw, dw, d2);
+          int t = min(gi * kGroup + k, nt - 1);
+          tu[k] = tgt[t];
+          tv[k] = tgt[kTileT + t];
+          tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : T(0);
+#pragma unroll
+          for (int v = 0; v < NV; v++) a[k][v] = T(0);
+        }
+        for (int j = lane; j < ncomp; j += 32) {
+          T su = comp[j], sv = comp[C::kComp + j];
+          T sw = DIM == 3 ? comp[2 * C::kComp + j] : T(0);
+          T sgj[NV];
+#pragma unroll
+          for (int v = 0; v < NV; v++) sgj[v] = comp[(DIM + v) * C::kComp + j];
+#pragma unroll
+          for (int k = 0; k < kGroup; k++) {
+            T du = tu[k] - su, dv = tv[k] - sv;
+            T d2 = du * du;
+            d2 = fma(dv, dv, d2);
+            if (DIM == 3) {
+              T dw = tw[k] - sw;
+              d2 = fma(dw, dw, d2);
+            }
+            if constexpr (F32) {
+              const float e = ex2_approx(-d2);
+#pragma unroll
+              for (int v = 0; v < NV; v++) a[k][v] = fmaf(sgj[v], e, a[k][v]);
+            } else {
+              // d2 = |x_t - x_s|^2 (unscaled: the differences are exact as in the reference);
+              // in units of L = ln2/kTab the exponent is kexp*d2, kexp = kTab/(2 sigma^2 ln2):
+              // k = rint(kexp d2) (fused), r = k - kexp d2 in [-1/2, 1/2] with a single rounding
+              const double magic = 6755399441055744.0;  // 1.5 * 2^52
+              double kd = fma(d2, kexp, magic);
+              int kk = __double2loint(kd);
+              double r = fma(-d2, kexp, kd - magic);
+              int j8 = kk & (kTab - 1);
+              // m <= 900 keeps every scaled coefficient normal (2^-900 ~ 1e-271)
+              int m20 = min(kk >> kTabBits, 900) << 20;
+              double q = hi_sub(tab[4 * kTab + j8], m20);
+              q = fma(r, q, hi_sub(tab[3 * kTab + j8], m20));
+              q = fma(r, q, hi_sub(tab[2 * kTab + j8], m20));
+              q = fma(r, q, hi_sub(tab[1 * kTab + j8], m20));
+              q = fma(r, q, hi_sub(tab[j8], m20));
+#pragma unroll
+              for (int v = 0; v < NV; v++) a[k][v] = fma(sgj[v], q, a[k][v]);
+            }
           }
-          if constexpr (F32) {
-            const float e = ex2_approx(-d2);
+        }
 #pragma unroll
-            for (int v = 0; v < NV; v++) a[k][v] = fmaf(sgj[v], e, a[k][v]);
-          } else {
-            // d2 = |x_t - x_s|^2 (unscaled: the differences are exact as in the reference);
-            // in units of L = ln2/kTab the exponent is kexp*d2, kexp = kTab/(2 sigma^2 ln2):
-            // k = rint(kexp d2) (fused), r = k - kexp d2 in [-1/2, 1/2] with a single rounding
-            const double magic = 6755399441055744.0;  // 1.5 * 2^52
-            double kd = fma(d2, kexp, magic);
-            int kk = __double2loint(kd);
-            double r = fma(-d2, kexp, kd - magic);
-            int j8 = kk & (kTab - 1);
-            // m <= 900 keeps every scaled coefficient normal (2^-900 ~ 1e-271)
-            int m20 = min(kk >> kTabBits, 900) << 20;
-            double q = hi_sub(tab[4 * kTab + j8], m20);
-            q = fma(r, q, hi_sub(tab[3 * kTab + j8], m20));
-            q = fma(r, q, hi_sub(tab[2 * kTab + j8], m20));
-            q = fma(r, q, hi_sub(tab[1 * kTab + j8], m20));
-            q = fma(r, q, hi_sub(tab[j8], m20));
+        for (int k = 0; k < kGroup; k++) {
+          int t = gi * kGroup + k;
 #pragma unroll
-            for (int v = 0; v < NV; v++) a[k][v] = fma(sgj[v], q, a[k][v]);
+          for (int v = 0; v < NV; v++) {
+            T s = warp_sum(a[k][v]);
+            if (lane == 0 && t < nt) acc[v * kTileT + t] += s;
           }
         }
       }
-#pragma unroll
-      for (int k = 0; k < kGroup; k++) {
-        int t = gi * kGroup + k;
-#pragma unroll
-        for (int v = 0; v < NV; v++) {
-          T s = warp_sum(a[k][v]);
-          if (lane == 0 && t < nt) acc[v * kTileT + t] += s;
-        }
-      }
-    }
-    ncomp = 0;
-  };
+      ncomp = 0;
+    };
 
-  while (true) {
-    // ---- plan and issue one fill (thread 0) -------------------------------------------
-    if (tid == 0) {
-      int r = s_cursor[0], p = s_cursor[1];
-      int used = 0, np = 0, valid = 0;
-      unsigned bytes = 0;
-      while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
-        int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
-        int a = cs_s[cell_of(g, jx, jy0, jz)], b = cs_s[cell_of(g, jx, jy1, jz) + 1];
-        int s = p < 0 ? a : p;
-        if (s >= b) {
-          r++;
-          p = -1;
-          continue;
-        }
-        int s_al = s & ~1;
-        int room = (kRawCap - used) & ~1;
-        int e_al = min((b + 1) & ~1, s_al + room);
-        int e = min(b, e_al);
-        pieces[np].raw_off = used + (s - s_al);
-        pieces[np].count = e - s;
-        pieces[np].gstart = s;
-        np++;
-        valid += e - s;
-        used += e_al - s_al;
-        bytes += (unsigned)(e_al - s_al) * 8u * NA;
-        if (e >= b) {
-          r++;
-          p = -1;
-        } else {
-          p = e;
-        }
-      }
-      s_cursor[0] = r;
-      s_cursor[1] = p;
-      s_fill[0] = np;
-      s_fill[1] = valid;
-      s_fill[2] = (np == 0);
-      if (np > 0) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(bar, bytes);
-        for (int q = 0; q < np; q++) {
-          int s = pieces[q].gstart, s_al = s & ~1;
-          int len = ((s + pieces[q].count + 1) & ~1) - s_al;
-          int dst = pieces[q].raw_off - (s - s_al);
-          bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
-          bulk_g2s(raw + kRawCap + dst, sy + s_al, len * 8u, bar);
-          if (DIM == 3) bulk_g2s(raw + 2 * kRawCap + dst, sz + s_al, len * 8u, bar);
-#pragma unroll
-          for (int v = 0; v < NV; v++) bulk_g2s(raw + (DIM + v) * kRawCap + dst, sg + v * vstride + s_al, len * 8u, bar);
-        }
-      }
-    }
-    __syncthreads();
-    if (s_fill[2]) break;
-    if (!mbar_wait(bar, phase)) {
+    while (true) {
+      // ---- plan and issue one fill (thread 0) -----------------------------------------
       if (tid == 0) {
-        atomicOr(err, DEV_ERR_TIMEOUT);
-        s_abort = 1;
+        int r = s_cursor[0], p = s_cursor[1];
+        int used = 0, np = 0, valid = 0;
+        unsigned bytes = 0;
+        while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
+          int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+          int a = cs_s[cb + cell_of(g, jx, jy0, jz)], b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
+          int s = p < 0 ? a : p;
+          if (s >= b) {
+            r++;
+            p = -1;
+            continue;
+          }
+          int s_al = s & ~1;
+          int room = (kRawCap - used) & ~1;
+          int e_al = min((b + 1) & ~1, s_al + room);
+          int e = min(b, e_al);
+          pieces[np].raw_off = used + (s - s_al);
+          pieces[np].count = e - s;
+          pieces[np].gstart = s;
+          np++;
+          valid += e - s;
+          used += e_al - s_al;
+          bytes += (unsigned)(e_al - s_al) * 8u * NA;
+          if (e >= b) {
+            r++;
+            p = -1;
+          } else {
+            p = e;
+          }
+        }
+        s_cursor[0] = r;
+        s_cursor[1] = p;
+        s_fill[0] = np;
+        s_fill[1] = valid;
+        s_fill[2] = (np == 0);
+        if (np > 0) {
+          fence_proxy_async_smem();
+          mbar_expect_tx(bar, bytes);
+          for (int q = 0; q < np; q++) {
+            int s = pieces[q].gstart, s_al = s & ~1;
+            int len = ((s + pieces[q].count + 1) & ~1) - s_al;
+            int dst = pieces[q].raw_off - (s - s_al);
+            bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
+            bulk_g2s(raw + kRawCap + dst, sy + s_al, len * 8u, bar);
+            if (DIM == 3) bulk_g2s(raw + 2 * kRawCap + dst, sz + s_al, len * 8u, bar);
+#pragma unroll
+            for (int v = 0; v < NV; v++)
+              bulk_g2s(raw + (DIM + v) * kRawCap + dst, sg + v * vstride + s_al, len * 8u, bar);
+          }
+        }
       }
-    }
-    phase ^= 1u;
-    __syncthreads();
-    if (s_abort) {
-      // let the copies of this fill land (bounded) before the CTA exits
-      mbar_wait(bar, phase ^ 1u, 1u << 20);
-      return;
-    }
-    // ---- make room, then filter + compact in order ----------------------------------
-    if (ncomp + s_fill[1] > C::kComp) {
-      flush();
       __syncthreads();
-    }
-    const int np = s_fill[0];
-    for (int q = 0; q < np; q++) {
-      const Piece pc = pieces[q];
-      for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
-        int e = e0 + tid;
-        bool in = false;
-        double vx = 0, vy = 0, vz = 0;
-        int ro = 0;
-        if (e < pc.count) {
-          int j = pc.gstart + e;
-          ro = pc.raw_off + e;
-          vx = raw[ro];
-          vy = raw[kRawCap + ro];
-          if (DIM == 3) vz = raw[2 * kRawCap + ro];
-          // centre cell unconditionally (2d/get_trunc.h:31-39), neighbours by the box test
-          // fabs(xj - xc) < trunc_length && ... (2d/get_trunc.h:63; 3d/get_trunc.h:70-72)
-          bool boxin = fabs(vx - xc) < L && fabs(vy - yc) < L;
-          if (DIM == 3) boxin = boxin && fabs(vz - zc) < L;
-          in = (j >= c0 && j < c1) || boxin;
+      if (s_fill[2]) break;
+      if (!mbar_wait(bar, phase)) {
+        if (tid == 0) {
+          atomicOr(err, DEV_ERR_TIMEOUT);
+          s_abort = 1;
         }
-        unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (lane == 0) s_wsum[wid] = __popc(bal);
-        __syncthreads();
-        int pre = 0, tot = 0;
-#pragma unroll
-        for (int k = 0; k < kWarps; k++) {
-          int c = s_wsum[k];
-          pre += k < wid ? c : 0;
-          tot += c;
-        }
-        if (in) {
-          int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
-          comp[pos] = (T)((vx - xc) * scale);
-          comp[C::kComp + pos] = (T)((vy - yc) * scale);
-          if (DIM == 3) comp[2 * C::kComp + pos] = (T)((vz - zc) * scale);
-#pragma unroll
-          for (int v = 0; v < NV; v++) comp[(DIM + v) * C::kComp + pos] = (T)raw[(DIM + v) * kRawCap + ro];
-        }
-        ncomp += tot;
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (s_abort) {
+        // let the copies of this fill land (bounded) before the CTA exits
+        mbar_wait(bar, phase ^ 1u, 1u << 20);
+        return;
+      }
+      // ---- make room, then filter + compact in order ----------------------------------
+      if (ncomp + s_fill[1] > C::kComp) {
+        flush();
         __syncthreads();
       }
-    }
-  }
-  flush();
-  __syncthreads();
-  for (int t = tid; t < nt; t += kThreads)
+      const int np = s_fill[0];
+      for (int q = 0; q < np; q++) {
+        const Piece pc = pieces[q];
+        for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
+          int e = e0 + tid;
+          bool in = false;
+          double vx = 0, vy = 0, vz = 0;
+          int ro = 0;
+          if (e < pc.count) {
+            int j = pc.gstart + e;
+            ro = pc.raw_off + e;
+            vx = raw[ro];
+            vy = raw[kRawCap + ro];
+            if (DIM == 3) vz = raw[2 * kRawCap + ro];
+            // centre cell unconditionally (2d/get_trunc.h:31-39), neighbours by the box test
+            // fabs(xj - xc) < trunc_length && ... (2d/get_trunc.h:63; 3d/get_trunc.h:70-72)
+            bool boxin = fabs(vx - xc) < L && fabs(vy - yc) < L;
+            if (DIM == 3) boxin = boxin && fabs(vz - zc) < L;
+            in = (j >= c0 && j < c1) || boxin;
+          }
+          unsigned bal = __ballot_sync(0xffffffffu, in);
+          if (lane == 0) s_wsum[wid] = __popc(bal);
+          __syncthreads();
+          int pre = 0, tot = 0;
 #pragma unroll
-    for (int v = 0; v < NV; v++) w[v * vstride + t0 + t] = (double)acc[v * kTileT + t] * norm;
+          for (int k = 0; k < kWarps; k++) {
+            int c = s_wsum[k];
+            pre += k < wid ? c : 0;
+            tot += c;
+          }
+          if (in) {
+            int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
+            comp[pos] = (T)((vx - xc) * scale);
+            comp[C::kComp + pos] = (T)((vy - yc) * scale);
+            if (DIM == 3) comp[2 * C::kComp + pos] = (T)((vz - zc) * scale);
+#pragma unroll
+            for (int v = 0; v < NV; v++) comp[(DIM + v) * C::kComp + pos] = (T)raw[(DIM + v) * kRawCap + ro];
+          }
+          ncomp += tot;
+          __syncthreads();
+        }
+      }
+    }
+    flush();
+    __syncthreads();
+    for (int t = tid; t < nt; t += kThreads)
+#pragma unroll
+      for (int v = 0; v < NV; v++) w[v * vstride + t0 + t] = (double)acc[v * kTileT + t] * kc.norm;
+  }
 }
 
 // ---- work list and truncation-set sizes ----------------------------------------------
@@ -425,7 +461,7 @@ size_t smem_bytes() {
   return Layout<DIM, F32, NV>::total;
 }
 
-template <int DIM, bool F32, int NV>
+template <int DIM, bool F32, int NV, bool BATCH>
 void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
             long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
   size_t sm = smem_bytes<DIM, F32, NV>();
@@ -434,33 +470,36 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
-    PRBF_CUDA(cudaFuncSetAttribute(k_gauss<DIM, F32, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PRBF_CUDA(
+        cudaFuncSetAttribute(k_gauss<DIM, F32, NV, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
-  const double sigma = P.g.sigma;
-  const double norm = 1.0 / (2 * M_PI * sigma * sigma);
   // FP32: coordinates scaled so that |dx|^2 is the exponent in units of ln2 (exp2).
   // FP64: unscaled cell-relative coordinates; kexp = kTab / (2 sigma^2 ln2) converts |dx|^2
   // to units of ln2/kTab inside the fused range reduction.
-  const double scale = F32 ? std::sqrt(1.0 / (2.0 * sigma * sigma * std::log(2.0))) : 1.0;
-  const double kexp = (double)kTab / (2.0 * sigma * sigma * std::log(2.0));
-  k_gauss<DIM, F32, NV><<<P.nitems, kThreads, sm, st>>>(P.g, P.items.get(), t.x, t.y, t.z, t.cell_start, s.x, s.y,
-                                                        s.z, gv, s.cell_start, w, vstride, scale, kexp, norm, err,
-                                                        skip);
+  const SumConsts k0 = sum_consts(P.g.sigma, F32);
+  const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
+  k_gauss<DIM, F32, NV, BATCH><<<grid, kThreads, sm, st>>>(P.g, P.grids.get(), P.cprob.get(), P.items.get(), P.nitems,
+                                                           t.x, t.y, t.z, t.cell_start, s.x, s.y, s.z, gv,
+                                                           s.cell_start, w, vstride, k0, P.seg, err, skip);
   PRBF_CHECK_LAUNCH();
 }
 
 template <int DIM, bool F32>
 void launch_nv(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w, int nv,
                long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
+  if (P.batched) {  // a batch of problems: the problems are the segments of one vector
+    for (int v = 0; v < nv; v++) launch<DIM, F32, 1, true>(P, t, s, gv + v * vstride, w + v * vstride, vstride, err, skip, st);
+    return;
+  }
   for (int v0 = 0; v0 < nv; v0 += 4) {
     const double* g0 = gv + v0 * vstride;
     double* w0 = w + v0 * vstride;
     switch (std::min(4, nv - v0)) {
-      case 1: launch<DIM, F32, 1>(P, t, s, g0, w0, vstride, err, skip, st); break;
-      case 2: launch<DIM, F32, 2>(P, t, s, g0, w0, vstride, err, skip, st); break;
-      case 3: launch<DIM, F32, 3>(P, t, s, g0, w0, vstride, err, skip, st); break;
-      default: launch<DIM, F32, 4>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      case 1: launch<DIM, F32, 1, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      case 2: launch<DIM, F32, 2, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      case 3: launch<DIM, F32, 3, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      default: launch<DIM, F32, 4, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
     }
   }
 }

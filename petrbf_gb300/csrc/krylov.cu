@@ -331,7 +331,7 @@ void Krylov::init(const std::vector<long long>& off_, const std::vector<int>& le
   total = total_;
   long long sum = 0;
   for (int i = 0; i < nseg; i++) {
-    if ((nseg > 1 && off[i] % 32) || len[i] < 0 || off[i] + len[i] > total) throw Error(PRBF_ERR_ARG, "bad segment");
+    if (off[i] < 0 || len[i] < 0 || off[i] + len[i] > total) throw Error(PRBF_ERR_ARG, "bad segment");
     sum += len[i];
   }
   ld = (total + 4 + 31) / 32 * 32;

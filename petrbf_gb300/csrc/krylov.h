@@ -70,8 +70,7 @@ struct Krylov {
   ~Krylov();
   // one system of n unknowns
   void init(int n, int m, cudaStream_t s);
-  // nseg systems; offsets must be multiples of 32 (aligned vector segments), total >= the
-  // end of the last segment
+  // nseg systems at the given offsets (non-overlapping; total >= the end of the last)
   void init(const std::vector<long long>& off, const std::vector<int>& len, long long total, int m, cudaStream_t s);
   bool same_layout(const std::vector<long long>& o, const std::vector<int>& l, int m_) const {
     return o == off && l == len && m_ == m;

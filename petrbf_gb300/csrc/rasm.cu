@@ -100,11 +100,13 @@ template <class T>
 __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const long long* __restrict__ boff,
                            const int* __restrict__ cs, const int* __restrict__ idx,
                            const long long* __restrict__ koff, const double* __restrict__ x,
-                           const double* __restrict__ y, const double* __restrict__ z, int dim, double inv2s2,
-                           double shift, T* __restrict__ K, const unsigned char* __restrict__ only) {
+                           const double* __restrict__ y, const double* __restrict__ z, int dim, double inv2s2_all,
+                           const double* __restrict__ cell_sig, double shift, T* __restrict__ K,
+                           const unsigned char* __restrict__ only) {
   int b = blockIdx.y;
   if (b >= nblk || (only && !only[b])) return;
   int c = blk_cell[b];
+  const double inv2s2 = cell_sig ? 1.0 / (2.0 * cell_sig[c] * cell_sig[c]) : inv2s2_all;
   int nbk = (int)(boff[c + 1] - boff[c]);
   int nc = cs[c + 1] - cs[c], n1 = nbk - nc;
   const int* id = idx + boff[c];
@@ -371,11 +373,20 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
                                                  const long long* __restrict__ koff, T* __restrict__ K,
                                                  const long long* __restrict__ xoff, T* __restrict__ Xw,
                                                  const long long* __restrict__ soff, T* __restrict__ Sout,
-                                                 double out_scale, unsigned char* __restrict__ bad,
+                                                 double out_scale_all, const double* __restrict__ cell_sig,
+                                                 unsigned char* __restrict__ bad,
                                                  const unsigned char* __restrict__ only, int mode,
                                                  const long long* __restrict__ loff, T* __restrict__ Lpack) {
   int b = blockIdx.x;
   if (b >= nblk || (only && !only[b])) return;
+  // per-block scale (batches of problems with their own sigma): mode 1 sqrt(1/(2 pi s^2)),
+  // mode 0 2 pi s^2
+  double out_scale = out_scale_all;
+  if (cell_sig) {
+    const double sg = cell_sig[blk_cell[b]];
+    const double two_pi_s2 = 2.0 * M_PI * sg * sg;
+    out_scale = mode == 1 ? sqrt(1.0 / two_pi_s2) : two_pi_s2;
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int S = SP<T>::S;
   constexpr int KC = KCOf<T>::v;
@@ -554,15 +565,18 @@ __global__ void __launch_bounds__(128) k_apply(int ncell, const long long* __res
 // triangle from shared memory, all warps update the rows below with coalesced row
 // segments), then the back substitution with L22^T only, since the centre unknowns are
 // the last n_c: x2 = L22^-T y2. With full set (basic Schwarz) the back substitution runs
-// over the whole block and every entry is added into out (zeroed beforehand): points lie
-// in several blocks, so the adds are atomic.
+// over the whole block and the whole solution goes to the block's slots of Y (slot =
+// position in the buffer list); k_asm_gather then sums each point's slots in block order,
+// so the result does not depend on the order the blocks ran in.
 template <class T>
 __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* __restrict__ boff,
                                                    const int* __restrict__ cs, const int* __restrict__ idx,
                                                    const long long* __restrict__ loff, const T* __restrict__ Lpack,
                                                    const double* __restrict__ r, double* __restrict__ out,
-                                                   const int* __restrict__ skip, int full) {
+                                                   const int* __restrict__ skip, int full, double* __restrict__ Y,
+                                                   SegSkip seg) {
   if (skip && *skip) return;
+  if (seg.cell_done(blockIdx.x)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tri[32][33];
   T* y = (T*)smem_raw;
@@ -651,16 +665,52 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     __syncthreads();
   }
   if (full) {
-    for (int j = tid; j < nb; j += blockDim.x) atomicAdd(&out[id[j < n1 ? nc + j : j - n1]], (double)y[j]);
+    double* Yc = Y + boff[c];
+    for (int j = tid; j < nb; j += blockDim.x) Yc[j < n1 ? nc + j : j - n1] = (double)y[j];
   } else {
     for (int i = tid; i < nc; i += blockDim.x) out[cs[c] + i] = (double)y2[i];
   }
 }
 
-__global__ void k_zero_unless(long long n, double* __restrict__ v, const int* __restrict__ skip) {
+// basic Schwarz: out[i] = sum of the slots of point i (ascending slot = ascending block)
+__global__ void k_asm_gather(int n, const long long* __restrict__ inv_off, const long long* __restrict__ inv_slot,
+                             const double* __restrict__ Y, double* __restrict__ out, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v[i] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (long long k = inv_off[i]; k < inv_off[i + 1]; k++) s += Y[inv_slot[k]];
+    out[i] = s;
+  }
+}
+
+// inverse of the buffer lists: per point, the slots that hold it
+__global__ void k_inv_count(long long nslot, const int* __restrict__ idx, long long* __restrict__ cnt) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nslot; k += (long long)gridDim.x * blockDim.x)
+    atomicAdd((unsigned long long*)&cnt[idx[k]], 1ull);
+}
+
+__global__ void k_inv_fill(long long nslot, const int* __restrict__ idx, const long long* __restrict__ off,
+                           long long* __restrict__ cur, long long* __restrict__ slot) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nslot; k += (long long)gridDim.x * blockDim.x) {
+    int i = idx[k];
+    long long p = (long long)atomicAdd((unsigned long long*)&cur[i], 1ull);
+    slot[off[i] + p] = k;
+  }
+}
+
+// each point's few slots in ascending order (insertion sort)
+__global__ void k_inv_sort(int n, const long long* __restrict__ off, long long* __restrict__ slot) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    long long a = off[i], e = off[i + 1];
+    for (long long k = a + 1; k < e; k++) {
+      long long v = slot[k], j = k - 1;
+      while (j >= a && slot[j] > v) {
+        slot[j + 1] = slot[j];
+        j--;
+      }
+      slot[j + 1] = v;
+    }
+  }
 }
 
 template <class T>
@@ -672,10 +722,7 @@ size_t chol_smem() {
 
 void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsigned* err, cudaStream_t s,
                 double ws_budget_bytes, bool factor, bool basic) {
-  (void)err;
   const Grid& g = P.g;
-  R.fp32 = fp32;
-  R.ncell = g.ncell;
   int* cnt = (int*)ws.get(40, sizeof(int) * ((size_t)g.ncell + 1));
   k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(), 0, cnt,
                                                       nullptr, nullptr);
@@ -684,54 +731,102 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
   PRBF_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, sizeof(int) * g.ncell, cudaMemcpyDeviceToHost, s));
   PRBF_CUDA(cudaMemcpyAsync(hcs.data(), P.cs.get(), sizeof(int) * (g.ncell + 1), cudaMemcpyDeviceToHost, s));
   PRBF_CUDA(cudaStreamSynchronize(s));
-  // host plan: offsets of buffer lists and S_c, the list of non-empty blocks
-  std::vector<long long> hb(g.ncell + 1), hso(g.ncell + 1);
+  std::vector<long long> hb(g.ncell + 1);
+  hb[0] = 0;
+  for (int c = 0; c < g.ncell; c++) hb[c + 1] = hb[c] + hcnt[c];
+  R.boff.reserve(g.ncell + 1);
+  R.idx.reserve(std::max<long long>(hb[g.ncell], 1));
+  PRBF_CUDA(cudaMemcpyAsync(R.boff.get(), hb.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
+  k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(), 1, cnt,
+                                                      R.boff.get(), R.idx.get());
+  PRBF_CHECK_LAUNCH();
+  BlockGeom G;
+  G.dim = g.dim;
+  G.n = P.n;
+  G.ncell = g.ncell;
+  G.x = P.x.get();
+  G.y = P.y.get();
+  G.z = P.view().z;
+  G.cs = P.cs.get();
+  G.sigma = g.sigma;
+  rasm_factor(R, G, hcnt, hcs, fp32, ws, err, s, ws_budget_bytes, factor, basic);
+}
+
+void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff_dev, int* idx_dev, cudaStream_t s) {
+  const Grid& g = P.g;
+  k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(),
+                                                      boff_dev ? 1 : 0, counts_dev, boff_dev, idx_dev);
+  PRBF_CHECK_LAUNCH();
+}
+
+void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, const std::vector<int>& hcs, bool fp32,
+                 Workspace& ws, unsigned* err, cudaStream_t s, double ws_budget_bytes, bool factor, bool basic) {
+  (void)err;
+  const int ncell = G.ncell;
+  R.fp32 = fp32;
+  R.ncell = ncell;
+  // host plan: offsets of S_c, the list of non-empty blocks (largest first, so the batches
+  // of the factorisation keep similar sizes together and the long blocks start early)
+  std::vector<long long> hso(ncell + 1);
   std::vector<int> blk;
-  hb[0] = hso[0] = 0;
+  hso[0] = 0;
   R.max_nb = 0;
   R.max_nc = 0;
-  for (int c = 0; c < g.ncell; c++) {
+  for (int c = 0; c < ncell; c++) {
     long long nbk = hcnt[c], nc = hcs[c + 1] - hcs[c];
-    hb[c + 1] = hb[c] + nbk;
     hso[c + 1] = hso[c] + nbk * nc;
     if (nbk) blk.push_back(c);
     R.max_nb = std::max<int>(R.max_nb, (int)nbk);
     R.max_nc = std::max<int>(R.max_nc, (int)nc);
   }
+  if (G.cell_sigma)
+    std::stable_sort(blk.begin(), blk.end(), [&](int a, int b) { return hcnt[a] > hcnt[b]; });
   R.nblocks = (int)blk.size();
-  R.boff.reserve(g.ncell + 1);
-  R.soff.reserve(g.ncell + 1);
-  R.idx.reserve(std::max<long long>(hb[g.ncell], 1));
-  PRBF_CUDA(cudaMemcpyAsync(R.boff.get(), hb.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
-  PRBF_CUDA(cudaMemcpyAsync(R.soff.get(), hso.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
-  k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(), 1, cnt,
-                                                      R.boff.get(), R.idx.get());
-  PRBF_CHECK_LAUNCH();
+  R.soff.reserve(ncell + 1);
+  PRBF_CUDA(cudaMemcpyAsync(R.soff.get(), hso.data(), sizeof(long long) * (ncell + 1), cudaMemcpyHostToDevice, s));
   size_t esz = fp32 ? sizeof(float) : sizeof(double);
   // FP64 form keeps the packed Cholesky factors (backward-stable triangular solves at
   // every apply); the FP32 form keeps S_c (one GEMV per apply)
   R.basic = basic;
-  R.n = P.n;
+  R.n = G.n;
   R.factor = !fp32 || factor || basic;
+  if (basic) {
+    // slots of each point (deterministic summation of the block solutions)
+    long long nslot = 0;
+    for (int c = 0; c < ncell; c++) nslot += hcnt[c];
+    R.Y.reserve(std::max<long long>(nslot, 1));
+    R.inv_off.reserve((size_t)G.n + 1);
+    R.inv_slot.reserve(std::max<long long>(nslot, 1));
+    long long* cur = (long long*)ws.get(47, sizeof(long long) * ((size_t)G.n + 1));
+    PRBF_CUDA(cudaMemsetAsync(R.inv_off.get(), 0, sizeof(long long) * ((size_t)G.n + 1), s));
+    PRBF_CUDA(cudaMemsetAsync(cur, 0, sizeof(long long) * ((size_t)G.n + 1), s));
+    const int gb = (int)std::max<long long>(1, std::min<long long>((nslot + 255) / 256, 8 * 152));
+    if (nslot) k_inv_count<<<gb, 256, 0, s>>>(nslot, R.idx.get(), R.inv_off.get());
+    PRBF_CHECK_LAUNCH();
+    scan_exclusive_dev(R.inv_off.get(), R.inv_off.get(), (long long)G.n + 1, ws, 48, s);
+    if (nslot) k_inv_fill<<<gb, 256, 0, s>>>(nslot, R.idx.get(), R.inv_off.get(), cur, R.inv_slot.get());
+    k_inv_sort<<<ceil_div(G.n, 256), 256, 0, s>>>(G.n, R.inv_off.get(), R.inv_slot.get());
+    PRBF_CHECK_LAUNCH();
+  }
   if (R.factor) {
-    std::vector<long long> hl(g.ncell + 1);
+    std::vector<long long> hl(ncell + 1);
     hl[0] = 0;
-    for (int c = 0; c < g.ncell; c++) hl[c + 1] = hl[c] + (long long)hcnt[c] * (hcnt[c] + 1) / 2;
-    R.loff.reserve(g.ncell + 1);
-    PRBF_CUDA(cudaMemcpyAsync(R.loff.get(), hl.data(), sizeof(long long) * (g.ncell + 1), cudaMemcpyHostToDevice, s));
+    for (int c = 0; c < ncell; c++) hl[c + 1] = hl[c] + (long long)hcnt[c] * (hcnt[c] + 1) / 2;
+    R.loff.reserve(ncell + 1);
+    PRBF_CUDA(cudaMemcpyAsync(R.loff.get(), hl.data(), sizeof(long long) * (ncell + 1), cudaMemcpyHostToDevice, s));
     if (fp32)
-      R.L32.reserve(std::max<long long>(hl[g.ncell], 1));
+      R.L32.reserve(std::max<long long>(hl[ncell], 1));
     else
-      R.L64.reserve(std::max<long long>(hl[g.ncell], 1));
+      R.L64.reserve(std::max<long long>(hl[ncell], 1));
     PRBF_CUDA(cudaStreamSynchronize(s));
   } else {
-    R.S32.reserve(std::max<long long>(hso[g.ncell], 1));
+    R.S32.reserve(std::max<long long>(hso[ncell], 1));
   }
 
   // batches of blocks within the workspace budget: K (nb^2), X (nb x ceil(nc/TB)TB) and
   // the diagonal inverses (ntile TB^2)
-  const double inv2s2 = 1.0 / (2.0 * g.sigma * g.sigma);
-  const double out_scale = 2.0 * M_PI * g.sigma * g.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
+  const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
+  const double out_scale = 2.0 * M_PI * G.sigma * G.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
   size_t smem = fp32 ? chol_smem<float>() : chol_smem<double>();
   if (fp32)
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -755,6 +850,7 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
       long long nct = (nc + TB - 1) / TB;
       long long ke = nbk * nbk, xe = R.factor ? 1 : nbk * nct * TB + ntile * TB * TB;
       if (!bc.empty() && (double)(hk.back() + ke + hx.back() + xe) * esz > ws_budget_bytes) break;
+      if (bc.size() >= 65535) break;  // gridDim.y of the assembly
       bc.push_back(c);
       hk.push_back(hk.back() + ke);
       hx.push_back(hx.back() + xe);
@@ -770,32 +866,31 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
     PRBF_CUDA(cudaMemcpyAsync(dbc, bc.data(), sizeof(int) * nb_batch, cudaMemcpyHostToDevice, s));
     PRBF_CUDA(cudaMemcpyAsync(dk, hk.data(), sizeof(long long) * (nb_batch + 1), cudaMemcpyHostToDevice, s));
     PRBF_CUDA(cudaMemcpyAsync(dx, hx.data(), sizeof(long long) * (nb_batch + 1), cudaMemcpyHostToDevice, s));
-    const double* zp = P.view().z;
     for (int attempt = 0; attempt < 3; attempt++) {
       const unsigned char* only = attempt ? dbad : nullptr;
       // diagonal shift of the retries (relative to the unit diagonal of K)
       double shift = attempt == 0 ? 0.0 : (fp32 ? (attempt == 1 ? 1e-5 : 1e-3) : (attempt == 1 ? 1e-12 : 1e-9));
       dim3 ag(64, nb_batch);
       if (fp32) {
-        k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
-                                             P.y.get(), zp, g.dim, inv2s2, shift, (float*)Kw, only);
+        k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
+                                             inv2s2, G.cell_sigma, shift, (float*)Kw, only);
         PRBF_CHECK_LAUNCH();
         if (R.factor)
-          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
+          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
                                                        (float*)Xw, R.soff.get(), nullptr, std::sqrt(1.0 / out_scale),
-                                                       dbad, only, 1, R.loff.get(), R.L32.get());
+                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get());
         else
-          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (float*)Kw, dx,
-                                                       (float*)Xw, R.soff.get(), R.S32.get(), out_scale, dbad,
-                                                       only, 0, nullptr, nullptr);
+          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
+                                                       (float*)Xw, R.soff.get(), R.S32.get(), out_scale,
+                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr);
       } else {
-        k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
-                                              P.y.get(), zp, g.dim, inv2s2, shift, (double*)Kw, only);
+        k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
+                                              G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only);
         PRBF_CHECK_LAUNCH();
-        k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), P.cs.get(), dk, (double*)Kw, dx,
+        k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (double*)Kw, dx,
                                                       (double*)Xw, R.soff.get(), nullptr,
-                                                      std::sqrt(1.0 / out_scale), dbad, only, 1, R.loff.get(),
-                                                      R.L64.get());
+                                                      std::sqrt(1.0 / out_scale), G.cell_sigma, dbad, only, 1,
+                                                      R.loff.get(), R.L64.get());
       }
       PRBF_CHECK_LAUNCH();
       hbad.resize(nb_batch);
@@ -814,21 +909,21 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
 void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s, const int* skip) {
   if (R.nblocks == 0) return;
   size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
-  if (R.basic) {
-    k_zero_unless<<<4 * 152, 256, 0, s>>>(R.n, out, skip);
-    PRBF_CHECK_LAUNCH();
-  }
   const int full = R.basic ? 1 : 0;
   if (R.factor && !R.fp32)
     k_apply_tri<double><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L64.get(), r,
-                                                 out, skip, full);
+                                                 out, skip, full, R.Y.get(), R.seg);
   else if (R.factor)
     k_apply_tri<float><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L32.get(), r,
-                                                out, skip, full);
+                                                out, skip, full, R.Y.get(), R.seg);
   else
     k_apply<float><<<R.ncell, 128, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.soff.get(), R.S32.get(), r, out,
                                             skip);
   PRBF_CHECK_LAUNCH();
+  if (R.basic) {
+    k_asm_gather<<<ceil_div(R.n, 256), 256, 0, s>>>(R.n, R.inv_off.get(), R.inv_slot.get(), R.Y.get(), out, skip);
+    PRBF_CHECK_LAUNCH();
+  }
 }
 
 void rasm_set_apply_smem(const RasmPlan& R) {

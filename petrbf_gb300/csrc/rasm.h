@@ -1,5 +1,7 @@
 // rasm.h -- restricted additive Schwarz preconditioner (rasm.cu).
 #pragma once
+#include <vector>
+
 #include "context.h"
 
 namespace prbf {
@@ -19,6 +21,10 @@ struct RasmPlan {
   DevBuf<double> L64;         // packed Cholesky factors (FP64 factor form), rows in block order
   DevBuf<float> L32;          // packed Cholesky factors (FP32 factor form)
   DevBuf<float> S32;          // S_c (FP32 inverse-rows form)
+  DevBuf<double> Y;           // basic form: block solutions, one slot per buffer-list entry
+  DevBuf<long long> inv_off;  // basic form: per point, its slots (n + 1 offsets)
+  DevBuf<long long> inv_slot; // basic form: the slots, ascending
+  SegSkip seg;                // batches: skip the blocks of stopped problems (when seg.done set)
 };
 
 // Buffer lists, blocks, factorisations and S_c for every non-empty cell of P.
@@ -29,6 +35,22 @@ struct RasmPlan {
 // the restricted form, z[centre(c)] = (A_c^-1 R_c r)[centre].
 void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsigned* err, cudaStream_t s,
                 double ws_budget_bytes, bool factor = false, bool basic = false);
+// Geometry of the blocks: cell-sorted points and cell starts (device, global indices),
+// with one sigma (single problem) or one per cell (a batch of problems).
+struct BlockGeom {
+  int dim = 2, n = 0, ncell = 0;
+  const double *x = nullptr, *y = nullptr, *z = nullptr;
+  const int* cs = nullptr;
+  double sigma = 0.0;
+  const double* cell_sigma = nullptr;
+};
+// Buffer lists of one grid (get_buffer): counts per cell when boff_dev is null, else the
+// lists at boff_dev (sorted positions of P, centre first).
+void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff_dev, int* idx_dev, cudaStream_t s);
+// Factorisation of every non-empty block, with R.boff / R.idx already in place (global
+// indices) and their host sizes: hcnt[c] block sizes, hcs the cell starts.
+void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, const std::vector<int>& hcs, bool fp32,
+                 Workspace& ws, unsigned* err, cudaStream_t s, double ws_budget_bytes, bool factor, bool basic);
 // Sets the dynamic shared memory limit of the apply kernel for this plan.
 void rasm_set_apply_smem(const RasmPlan& R);
 // Restricted: out[centre(c)] = (A_c^-1 r[buffer(c)])[centre] for every cell; basic:

@@ -65,6 +65,8 @@ Ctx::~Ctx() {
   solve = nullptr;
   delete guess;
   guess = nullptr;
+  batch_state_free(batch);
+  batch = nullptr;
   ctx_stream_release(*this);
 }
 

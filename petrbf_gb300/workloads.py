@@ -125,6 +125,31 @@ def config3(m=128, seed=12345, nsigma_box=2):
                    meta={"m": m, "h": h, "jitter": 0.25, "seed": seed})
 
 
+def config4(nprob=256, seed=2024, nmin=2000, nmax=200000, nsigma_box=4):
+    """Batched 2D: nprob independent problems, N log-uniform in [nmin, nmax], points
+    uniform-random in [-1,1]^2, h = 2/sqrt(N), h/sigma uniform in [0.6, 1.0], Lamb-Oseen
+    right-hand side (G = 1, t = 1) with centre uniform in [-0.5,0.5]^2 and core radius
+    r_c = sqrt(4 nu t) uniform in [0.1, 0.3]. Cell nsigma_box sigma (blocks of one cell
+    plus a one-cell buffer, 3 nsigma_box sigma wide), cutoff 8 sigma past the cell edge.
+    Returns a list of problem dicts (the batch_interpolate input) with their metadata."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nprob):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        x = rng.uniform(-1.0, 1.0, n)
+        y = rng.uniform(-1.0, 1.0, n)
+        h = 2.0 / math.sqrt(n)
+        ratio = rng.uniform(0.6, 1.0)
+        xc, yc = rng.uniform(-0.5, 0.5, 2)
+        rc = rng.uniform(0.1, 0.3)
+        nu = rc * rc / 4.0
+        f = lamb_oseen(x, y, nu=nu, xc=xc, yc=yc)
+        out.append({"x": x, "y": y, "f": f, "sigma": h / ratio, "nsigma_box": nsigma_box,
+                    "sigma_buffer": 3 * nsigma_box, "sigma_trunc": nsigma_box + 16,
+                    "meta": {"n": n, "h_over_sigma": ratio, "centre": (xc, yc), "core_radius": rc}})
+    return out
+
+
 def log10_rel_error(w, e):
     """log10(||w - e||_2 / ||e||_2), 2d/main.cxx:130-133."""
     w = np.asarray(w, np.float64)
