@@ -93,6 +93,13 @@ struct GaussPlan {
   DevBuf<Grid> grids;     // batched: one grid per problem (with its first global cell)
   DevBuf<int> cprob;      // batched: problem of each global cell
   SegSkip seg;            // batched: skip the items of stopped problems (when seg.done set)
+  // FP32 form: per-source FP32 cell-relative coordinates and truncation masks (built by
+  // gauss_plan_dev when nb_trunc <= 7 and ny < 65536), and a FP32 copy of <= 4 weight
+  // vectors at stride g32_stride
+  bool f32_ready = false;
+  long long g32_stride = 0;
+  DevBuf<float> su, sv, sw, g32;
+  DevBuf<unsigned long long> smask;
 };
 
 // Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc.

@@ -38,6 +38,7 @@ constexpr int kTileT = 128;    // targets per work item
 constexpr int kGroup = 4;      // targets per warp pass
 constexpr int kRawCap = 1024;  // staged raw sources per fill (incl. alignment padding)
 constexpr int kMaxPieces = 64; // source ranges per fill
+constexpr int kMaxRanges = 256; // column ranges of an item kept in shared memory
 
 // exp table: e^a with a = -L*d, d >= 0, L = ln2/kTab:  k = rint(d), r = k - d in [-1/2, 1/2],
 // e^a = 2^(-k/kTab) e^(L r) = 2^-m T[j] sum_i (L r)^i / i!,  k = m*kTab + j.
@@ -130,6 +131,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   __shared__ int s_fill[3];  // npieces, valid total, done flag
   __shared__ int s_cursor[2];
   __shared__ int s_abort;
+  __shared__ int s_ra[kMaxRanges], s_rb[kMaxRanges];  // source ranges of the item's columns
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   if (!F32)
@@ -168,6 +170,12 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
     const int nranges = ncolx * (jz1 - jz0 + 1);
 
     __syncthreads();  // the previous item's readers of tgt/acc/comp are done
+    // the column ranges, loaded by all threads at once (thread 0 plans the fills from them)
+    for (int r = tid; r < min(nranges, kMaxRanges); r += kThreads) {
+      const int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+      s_ra[r] = cs_s[cb + cell_of(g, jx, jy0, jz)];
+      s_rb[r] = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
+    }
     for (int t = tid; t < nt; t += kThreads) {
       tgt[t] = (T)((tx[t0 + t] - xc) * scale);
       tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
@@ -260,7 +268,14 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
         unsigned bytes = 0;
         while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
           int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
-          int a = cs_s[cb + cell_of(g, jx, jy0, jz)], b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
+          int a, b;
+          if (r < kMaxRanges) {
+            a = s_ra[r];
+            b = s_rb[r];
+          } else {
+            a = cs_s[cb + cell_of(g, jx, jy0, jz)];
+            b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
+          }
           int s = p < 0 ? a : p;
           if (s >= b) {
             r++;
@@ -377,6 +392,315 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   }
 }
 
+// ---- FP32 form with precomputed source data ------------------------------------------
+// Once per point set, for every source j of cell (jx, jy, jz): FP32 coordinates relative
+// to its own cell centre, scaled (u, v, w), and a 64-bit word holding, per axis, bit k
+// (k = 0 .. 2 nb) = the reference's FP64 box test |x_j - xc| < trunc_len against the
+// centre of the target cell at offset k - nb from the source's cell (the same arithmetic
+// as the FP64 kernel, so the truncation set is identical), and jy in the top 16 bits. The
+// per-source filter is then integer work and the target-relative coordinate is
+// u_j + (jx - ix) box scale, one FP32 add (the FP64 path rounds once from FP64 instead).
+constexpr int kMaskBits = 15;    // 2 nb + 1 <= 15 bits per axis: nb_trunc <= 7
+constexpr int kMaskY = kMaskBits, kMaskZ = 2 * kMaskBits, kMaskCellY = 48;
+constexpr int kAlignF = 4;       // elements per 16 bytes (FP32 arrays; the masks use 2 x 16)
+
+__global__ void k_src_f32(Grid g, const int* __restrict__ cs, const double* __restrict__ x,
+                          const double* __restrict__ y, const double* __restrict__ z, double scale,
+                          float* __restrict__ U, float* __restrict__ V, float* __restrict__ W,
+                          unsigned long long* __restrict__ M) {
+  const int nb = g.nb_trunc;
+  const double L = g.trunc_len;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    cell_xyz(g, c, ix, iy, iz);
+    const double xc = centre_coord(g.xmin, ix, g.box), yc = centre_coord(g.ymin, iy, g.box);
+    const double zc = g.dim == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+    for (int j = cs[c]; j < cs[c + 1]; j++) {
+      unsigned long long m = (unsigned long long)iy << kMaskCellY;
+      for (int k = 0; k <= 2 * nb; k++) {
+        const int o = k - nb;  // source cell - target cell
+        if (fabs(x[j] - centre_coord(g.xmin, ix - o, g.box)) < L) m |= 1ull << k;
+        if (fabs(y[j] - centre_coord(g.ymin, iy - o, g.box)) < L) m |= 1ull << (kMaskY + k);
+        if (g.dim == 3 && fabs(z[j] - centre_coord(g.zmin, iz - o, g.box)) < L) m |= 1ull << (kMaskZ + k);
+      }
+      U[j] = (float)((x[j] - xc) * scale);
+      V[j] = (float)((y[j] - yc) * scale);
+      if (g.dim == 3) W[j] = (float)((z[j] - zc) * scale);
+      M[j] = m;
+    }
+  }
+}
+
+__global__ void k_to_f32(int n, int nv, long long vs_in, long long vs_out, const double* __restrict__ in,
+                         float* __restrict__ out, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (int v = 0; v < nv; v++)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+      out[v * vs_out + i] = (float)in[v * vs_in + i];
+}
+
+template <int DIM, int NV>
+struct LayoutF {
+  static constexpr int NF = DIM + NV;  // FP32 staged arrays: coordinates + weights
+  static constexpr int kComp = 2048;
+  static constexpr size_t rawf = 0;
+  static constexpr size_t rawm = align16(rawf + sizeof(float) * NF * kRawCap);
+  static constexpr size_t comp = align16(rawm + sizeof(unsigned long long) * kRawCap);
+  static constexpr size_t tgt = align16(comp + sizeof(float) * NF * kComp);
+  static constexpr size_t acc = align16(tgt + sizeof(float) * DIM * kTileT);
+  static constexpr size_t pieces = align16(acc + sizeof(float) * NV * kTileT);
+  static constexpr size_t bar = align16(pieces + sizeof(Piece) * kMaxPieces);
+  static constexpr size_t total = bar + 16;
+};
+
+template <int DIM, int NV>
+__global__ void __launch_bounds__(kThreads) k_gauss_f32m(
+    Grid g, const int2* __restrict__ items, int nitems, const double* __restrict__ tx, const double* __restrict__ ty,
+    const double* __restrict__ tz, const int* __restrict__ cs_t, const float* __restrict__ su,
+    const float* __restrict__ sv, const float* __restrict__ sw, const unsigned long long* __restrict__ smask,
+    const float* __restrict__ sg, long long vs_g, const int* __restrict__ cs_s, double* __restrict__ w,
+    long long vs_w, double scale, double norm, unsigned* err, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  using Lay = LayoutF<DIM, NV>;
+  constexpr int NF = Lay::NF, KC = Lay::kComp;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* rawf = (float*)(smem + Lay::rawf);                           // NF x kRawCap
+  unsigned long long* rawm = (unsigned long long*)(smem + Lay::rawm);  // kRawCap
+  float* comp = (float*)(smem + Lay::comp);                           // NF x KC
+  float* tgt = (float*)(smem + Lay::tgt);                             // DIM x kTileT
+  float* acc = (float*)(smem + Lay::acc);                             // NV x kTileT
+  Piece* pieces = (Piece*)(smem + Lay::pieces);
+  uint64_t* bar = (uint64_t*)(smem + Lay::bar);
+  __shared__ int s_wsum[kWarps];
+  __shared__ int s_fill[3];
+  __shared__ int s_cursor[2];
+  __shared__ int s_abort;
+  __shared__ int s_ra[kMaxRanges], s_rb[kMaxRanges];  // source ranges of the item's columns
+  __shared__ int s_prange[kMaxPieces];  // range index of each piece
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) mbar_init(bar, 1);
+  unsigned phase = 0;
+  const int G = gridDim.x;
+  const float boxs = (float)(g.box * scale);
+  const int nb = g.nb_trunc;
+
+  for (int round = 0; (long long)round * G < nitems; round++) {
+    const int it = (round & 1) ? round * G + (G - 1 - (int)blockIdx.x) : round * G + (int)blockIdx.x;
+    if (it >= nitems) continue;
+    const int2 item = items[it];
+    const int ic = item.x, t0 = item.y;
+    const int nt = min(kTileT, cs_t[ic + 1] - t0);
+    int ix, iy, iz;
+    cell_xyz(g, ic, ix, iy, iz);
+    const double xc = centre_coord(g.xmin, ix, g.box);
+    const double yc = centre_coord(g.ymin, iy, g.box);
+    const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+    const int c0 = cs_s[ic], c1 = cs_s[ic + 1];
+    const int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+    const int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+    const int jz0 = DIM == 3 ? max(0, iz - nb) : 0, jz1 = DIM == 3 ? min(g.nz - 1, iz + nb) : 0;
+    const int ncolx = jx1 - jx0 + 1;
+    const int nranges = ncolx * (jz1 - jz0 + 1);
+
+    __syncthreads();
+    for (int r = tid; r < min(nranges, kMaxRanges); r += kThreads) {
+      const int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+      s_ra[r] = cs_s[cell_of(g, jx, jy0, jz)];
+      s_rb[r] = cs_s[cell_of(g, jx, jy1, jz) + 1];
+    }
+    for (int t = tid; t < nt; t += kThreads) {
+      tgt[t] = (float)((tx[t0 + t] - xc) * scale);
+      tgt[kTileT + t] = (float)((ty[t0 + t] - yc) * scale);
+      if (DIM == 3) tgt[2 * kTileT + t] = (float)((tz[t0 + t] - zc) * scale);
+#pragma unroll
+      for (int v = 0; v < NV; v++) acc[v * kTileT + t] = 0.f;
+    }
+    if (tid == 0) {
+      s_cursor[0] = 0;
+      s_cursor[1] = -1;
+      s_abort = 0;
+    }
+    __syncthreads();
+
+    int ncomp = 0;
+    const int ngroups = (nt + kGroup - 1) / kGroup;
+    auto flush = [&]() {
+      for (int gi = wid; gi < ngroups; gi += kWarps) {
+        float tu[kGroup], tv[kGroup], tw[kGroup], a[kGroup][NV];
+#pragma unroll
+        for (int k = 0; k < kGroup; k++) {
+          int t = min(gi * kGroup + k, nt - 1);
+          tu[k] = tgt[t];
+          tv[k] = tgt[kTileT + t];
+          tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : 0.f;
+#pragma unroll
+          for (int v = 0; v < NV; v++) a[k][v] = 0.f;
+        }
+        for (int j = lane; j < ncomp; j += 32) {
+          const float cu = comp[j], cv = comp[KC + j], cw = DIM == 3 ? comp[2 * KC + j] : 0.f;
+          float gj[NV];
+#pragma unroll
+          for (int v = 0; v < NV; v++) gj[v] = comp[(DIM + v) * KC + j];
+#pragma unroll
+          for (int k = 0; k < kGroup; k++) {
+            float du = tu[k] - cu, dv = tv[k] - cv;
+            float d2 = fmaf(dv, dv, du * du);
+            if (DIM == 3) {
+              float dw = tw[k] - cw;
+              d2 = fmaf(dw, dw, d2);
+            }
+            const float e = ex2_approx(-d2);
+#pragma unroll
+            for (int v = 0; v < NV; v++) a[k][v] = fmaf(gj[v], e, a[k][v]);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kGroup; k++) {
+          int t = gi * kGroup + k;
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            float sm = warp_sum(a[k][v]);
+            if (lane == 0 && t < nt) acc[v * kTileT + t] += sm;
+          }
+        }
+      }
+      ncomp = 0;
+    };
+
+    while (true) {
+      if (tid == 0) {
+        int r = s_cursor[0], p = s_cursor[1];
+        int used = 0, np = 0, valid = 0;
+        unsigned bytes = 0;
+        while (r < nranges && np < kMaxPieces && kRawCap - used >= kAlignF) {
+          int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+          int a, b;
+          if (r < kMaxRanges) {
+            a = s_ra[r];
+            b = s_rb[r];
+          } else {
+            a = cs_s[cell_of(g, jx, jy0, jz)];
+            b = cs_s[cell_of(g, jx, jy1, jz) + 1];
+          }
+          int s = p < 0 ? a : p;
+          if (s >= b) {
+            r++;
+            p = -1;
+            continue;
+          }
+          int s_al = s & ~(kAlignF - 1);
+          int room = (kRawCap - used) & ~(kAlignF - 1);
+          int e_al = min((b + kAlignF - 1) & ~(kAlignF - 1), s_al + room);
+          int e = min(b, e_al);
+          pieces[np].raw_off = used + (s - s_al);
+          pieces[np].count = e - s;
+          pieces[np].gstart = s;
+          s_prange[np] = r;
+          np++;
+          valid += e - s;
+          used += e_al - s_al;
+          bytes += (unsigned)(e_al - s_al) * (4u * NF + 8u);
+          if (e >= b) {
+            r++;
+            p = -1;
+          } else {
+            p = e;
+          }
+        }
+        s_cursor[0] = r;
+        s_cursor[1] = p;
+        s_fill[0] = np;
+        s_fill[1] = valid;
+        s_fill[2] = (np == 0);
+        if (np > 0) {
+          fence_proxy_async_smem();
+          mbar_expect_tx(bar, bytes);
+          for (int q = 0; q < np; q++) {
+            int s = pieces[q].gstart, s_al = s & ~(kAlignF - 1);
+            int len = ((s + pieces[q].count + kAlignF - 1) & ~(kAlignF - 1)) - s_al;
+            int dst = pieces[q].raw_off - (s - s_al);
+            bulk_g2s(rawf + dst, su + s_al, len * 4u, bar);
+            bulk_g2s(rawf + kRawCap + dst, sv + s_al, len * 4u, bar);
+            if (DIM == 3) bulk_g2s(rawf + 2 * kRawCap + dst, sw + s_al, len * 4u, bar);
+#pragma unroll
+            for (int v = 0; v < NV; v++) bulk_g2s(rawf + (DIM + v) * kRawCap + dst, sg + v * vs_g + s_al, len * 4u, bar);
+            bulk_g2s(rawm + dst, smask + s_al, len * 8u, bar);
+          }
+        }
+      }
+      __syncthreads();
+      if (s_fill[2]) break;
+      if (!mbar_wait(bar, phase)) {
+        if (tid == 0) {
+          atomicOr(err, DEV_ERR_TIMEOUT);
+          s_abort = 1;
+        }
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (s_abort) {
+        mbar_wait(bar, phase ^ 1u, 1u << 20);
+        return;
+      }
+      if (ncomp + s_fill[1] > KC) {
+        flush();
+        __syncthreads();
+      }
+      const int np = s_fill[0];
+      for (int q = 0; q < np; q++) {
+        const Piece pc = pieces[q];
+        const int r = s_prange[q];
+        const int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
+        const int kx = jx - ix + nb, kz = jz - iz + nb;
+        const float offx = (float)(jx - ix) * boxs, offz = (float)(jz - iz) * boxs;
+        for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
+          int e = e0 + tid;
+          bool in = false;
+          int ro = 0;
+          unsigned long long m = 0;
+          if (e < pc.count) {
+            const int j = pc.gstart + e;
+            ro = pc.raw_off + e;
+            m = rawm[ro];
+            const int ky = (int)(m >> kMaskCellY) - iy + nb;
+            bool boxin = ((m >> kx) & (m >> (kMaskY + ky)) & 1ull) != 0;
+            if (DIM == 3) boxin = boxin && ((m >> (kMaskZ + kz)) & 1ull);
+            // centre cell unconditionally (2d/get_trunc.h:31-39)
+            in = (j >= c0 && j < c1) || boxin;
+          }
+          unsigned bal = __ballot_sync(0xffffffffu, in);
+          if (lane == 0) s_wsum[wid] = __popc(bal);
+          __syncthreads();
+          int pre = 0, tot = 0;
+#pragma unroll
+          for (int k = 0; k < kWarps; k++) {
+            int c = s_wsum[k];
+            pre += k < wid ? c : 0;
+            tot += c;
+          }
+          if (in) {
+            int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
+            const int jy = (int)(m >> kMaskCellY);
+            comp[pos] = rawf[ro] + offx;
+            comp[KC + pos] = rawf[kRawCap + ro] + (float)(jy - iy) * boxs;
+            if (DIM == 3) comp[2 * KC + pos] = rawf[2 * kRawCap + ro] + offz;
+#pragma unroll
+            for (int v = 0; v < NV; v++) comp[(DIM + v) * KC + pos] = rawf[(DIM + v) * kRawCap + ro];
+          }
+          ncomp += tot;
+          __syncthreads();
+        }
+      }
+    }
+    flush();
+    __syncthreads();
+    for (int t = tid; t < nt; t += kThreads)
+#pragma unroll
+      for (int v = 0; v < NV; v++) w[v * vs_w + t0 + t] = (double)acc[v * kTileT + t] * norm;
+  }
+}
+
 // ---- work list and truncation-set sizes ----------------------------------------------
 __global__ void k_item_counts(int ncell, const int* __restrict__ cs_t, int* __restrict__ cnt) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -485,9 +809,45 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   PRBF_CHECK_LAUNCH();
 }
 
+template <int DIM, int NV>
+void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
+                 long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
+  constexpr size_t sm = LayoutF<DIM, NV>::total;
+  static_assert(sm <= 227 * 1024, "k_gauss_f32m shared memory");
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  PRBF_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !attr_set[dev]) {
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_f32m<DIM, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (dev < 64) attr_set[dev] = true;
+  }
+  const SumConsts k0 = sum_consts(P.g.sigma, true);
+  k_to_f32<<<4 * 152, 256, 0, st>>>(s.n, NV, vstride, P.g32_stride, gv, P.g32.get(), skip);
+  PRBF_CHECK_LAUNCH();
+  const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
+  k_gauss_f32m<DIM, NV><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, t.x, t.y, t.z, t.cell_start,
+                                                     P.su.get(), P.sv.get(), P.sw.get(), P.smask.get(), P.g32.get(),
+                                                     P.g32_stride, s.cell_start, w, vstride, k0.scale, k0.norm, err,
+                                                     skip);
+  PRBF_CHECK_LAUNCH();
+}
+
 template <int DIM, bool F32>
 void launch_nv(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w, int nv,
                long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
+  if (F32 && P.f32_ready && !P.batched) {
+    for (int v0 = 0; v0 < nv; v0 += 4) {
+      const double* g0 = gv + v0 * vstride;
+      double* w0 = w + v0 * vstride;
+      switch (std::min(4, nv - v0)) {
+        case 1: launch_f32m<DIM, 1>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        case 2: launch_f32m<DIM, 2>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        case 3: launch_f32m<DIM, 3>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        default: launch_f32m<DIM, 4>(P, t, s, g0, w0, vstride, err, skip, st); break;
+      }
+    }
+    return;
+  }
   if (P.batched) {  // a batch of problems: the problems are the segments of one vector
     for (int v = 0; v < nv; v++) launch<DIM, F32, 1, true>(P, t, s, gv + v * vstride, w + v * vstride, vstride, err, skip, st);
     return;
@@ -540,6 +900,26 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
   plan.max_trunc = h.maxc;
   plan.max_tile = kTileT;
   upload_table(s);
+  // FP32 form's source data
+  plan.f32_ready = false;
+  if (2 * g.nb_trunc + 1 <= kMaskBits && g.ny < 65536 && src.n > 0) {
+    const long long n8 = (long long)src.n + 8;
+    plan.su.reserve(n8);
+    plan.sv.reserve(n8);
+    plan.sw.reserve(g.dim == 3 ? n8 : 1);
+    plan.smask.reserve(n8);
+    plan.g32_stride = ((long long)src.n + 8 + 31) / 32 * 32;
+    plan.g32.reserve(4 * plan.g32_stride);
+    PRBF_CUDA(cudaMemsetAsync(plan.g32.get(), 0, sizeof(float) * 4 * plan.g32_stride, s));
+    for (auto* b : {&plan.su, &plan.sv}) PRBF_CUDA(cudaMemsetAsync(b->get(), 0, sizeof(float) * n8, s));
+    if (g.dim == 3) PRBF_CUDA(cudaMemsetAsync(plan.sw.get(), 0, sizeof(float) * n8, s));
+    PRBF_CUDA(cudaMemsetAsync(plan.smask.get(), 0, sizeof(unsigned long long) * n8, s));
+    const SumConsts k32 = sum_consts(g.sigma, true);
+    k_src_f32<<<ceil_div(g.ncell, 128), 128, 0, s>>>(g, src.cell_start, src.x, src.y, src.z, k32.scale,
+                                                     plan.su.get(), plan.sv.get(), plan.sw.get(), plan.smask.get());
+    PRBF_CHECK_LAUNCH();
+    plan.f32_ready = true;
+  }
 }
 
 void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv,

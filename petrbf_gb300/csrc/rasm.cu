@@ -567,27 +567,32 @@ __global__ void __launch_bounds__(128) k_apply(int ncell, const long long* __res
 // the last n_c: x2 = L22^-T y2. With full set (basic Schwarz) the back substitution runs
 // over the whole block and the whole solution goes to the block's slots of Y (slot =
 // position in the buffer list); k_asm_gather then sums each point's slots in block order,
-// so the result does not depend on the order the blocks ran in.
-template <class T>
+// so the result does not depend on the order the blocks ran in. NV right-hand sides
+// (vectors at stride vs, slots at stride ys) share every load of the factor.
+template <class T, int NV>
 __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* __restrict__ boff,
                                                    const int* __restrict__ cs, const int* __restrict__ idx,
                                                    const long long* __restrict__ loff, const T* __restrict__ Lpack,
                                                    const double* __restrict__ r, double* __restrict__ out,
-                                                   const int* __restrict__ skip, int full, double* __restrict__ Y,
-                                                   SegSkip seg) {
+                                                   long long vs, const int* __restrict__ skip, int full,
+                                                   double* __restrict__ Y, long long ys, SegSkip seg) {
   if (skip && *skip) return;
   if (seg.cell_done(blockIdx.x)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tri[32][33];
-  T* y = (T*)smem_raw;
   const int c = blockIdx.x;
   const int nb = (int)(boff[c + 1] - boff[c]);
   if (nb == 0) return;
+  T* y = (T*)smem_raw;  // NV x nb
   const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
   const int* id = idx + boff[c];
   const T* L = Lpack + loff[c];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
-  for (int j = tid; j < nb; j += blockDim.x) y[j] = (T)r[id[j < n1 ? nc + j : j - n1]];
+  for (int j = tid; j < nb; j += blockDim.x) {
+    const int p = id[j < n1 ? nc + j : j - n1];
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v * nb + j] = (T)r[v * vs + p];
+  }
   __syncthreads();
   // forward: L y = r
   for (int p0 = 0; p0 < nb; p0 += 32) {
@@ -598,13 +603,21 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     }
     __syncthreads();
     if (w == 0) {
-      T ri = lane < np ? y[p0 + lane] : T(0);
+      T ri[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) ri[v] = lane < np ? y[v * nb + p0 + lane] : T(0);
       for (int j = 0; j < np; j++) {
-        if (lane == j) ri = ri * tri[j][j];  // reciprocal diagonal
-        T yj = __shfl_sync(0xffffffffu, ri, j);
-        if (lane > j) ri = fma(-tri[lane][j], yj, ri);
+        const T d = tri[j][j], l = tri[lane][j];
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          if (lane == j) ri[v] = ri[v] * d;  // reciprocal diagonal
+          T yj = __shfl_sync(0xffffffffu, ri[v], j);
+          if (lane > j) ri[v] = fma(-l, yj, ri[v]);
+        }
       }
-      if (lane < np) y[p0 + lane] = ri;
+      if (lane < np)
+#pragma unroll
+        for (int v = 0; v < NV; v++) y[v * nb + p0 + lane] = ri[v];
     }
     __syncthreads();
     // rows below the panel: y[i] -= L[i][p0 .. p0+np) . y[p0 ..]. Four lanes per row, each
@@ -612,28 +625,40 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     // narrow FP64 pipe a full warp reduction per row would cost 5x the row's FMAs.
     {
       const int sub = lane & 3, rw = lane >> 2;
-      T ys[8];
+      T ysv[NV][8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) ys[q] = (sub * 8 + q < np) ? y[p0 + sub * 8 + q] : T(0);
+      for (int v = 0; v < NV; v++)
+#pragma unroll
+        for (int q = 0; q < 8; q++) ysv[v][q] = (sub * 8 + q < np) ? y[v * nb + p0 + sub * 8 + q] : T(0);
       for (int i0 = p0 + np + 8 * w; i0 < nb; i0 += 8 * nw) {
         const long long i = i0 + rw;
-        T acc = T(0);
+        T acc[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) acc[v] = T(0);
         if (i < nb) {
           const T* Li = L + i * (i + 1) / 2 + p0 + sub * 8;
 #pragma unroll
           for (int q = 0; q < 8; q++)
-            if (sub * 8 + q < np) acc = fma(Li[q], ys[q], acc);
+            if (sub * 8 + q < np) {
+              const T lv = Li[q];
+#pragma unroll
+              for (int v = 0; v < NV; v++) acc[v] = fma(lv, ysv[v][q], acc[v]);
+            }
         }
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (sub == 0 && i < nb) y[i] -= acc;
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], 1);
+          acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], 2);
+        }
+        if (sub == 0 && i < nb)
+#pragma unroll
+          for (int v = 0; v < NV; v++) y[v * nb + i] -= acc[v];
       }
     }
     __syncthreads();
   }
   // backward on the trailing block (rows b0 ..): L22^T x2 = y2, panels from the bottom
   const int b0 = full ? 0 : n1, nback = nb - b0;
-  T* y2 = y + b0;
   for (int pe = nback; pe > 0; pe -= 32) {
     const int p0 = max(0, pe - 32), np = pe - p0;
     // tri[i][j] = L22[p0 + i][p0 + j], j <= i
@@ -644,43 +669,62 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     }
     __syncthreads();
     if (w == 0) {  // x_i = (y_i - sum_{j > i} L22[j][i] x_j) / L22[i][i], i = np-1 .. 0
-      T xi = lane < np ? y2[p0 + lane] : T(0);
+      T xi[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) xi[v] = lane < np ? y[v * nb + b0 + p0 + lane] : T(0);
       for (int j = np - 1; j >= 0; j--) {
-        if (lane == j) xi = xi * tri[j][j];  // reciprocal diagonal
-        T xj = __shfl_sync(0xffffffffu, xi, j);
-        if (lane < j) xi = fma(-tri[j][lane], xj, xi);
+        const T d = tri[j][j], l = tri[j][lane];
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          if (lane == j) xi[v] = xi[v] * d;  // reciprocal diagonal
+          T xj = __shfl_sync(0xffffffffu, xi[v], j);
+          if (lane < j) xi[v] = fma(-l, xj, xi[v]);
+        }
       }
-      if (lane < np) y2[p0 + lane] = xi;
+      if (lane < np)
+#pragma unroll
+        for (int v = 0; v < NV; v++) y[v * nb + b0 + p0 + lane] = xi[v];
     }
     __syncthreads();
     // rows above the panel: y2[k] -= sum_{j in panel} L22[p0 + j][k] x_j, k < p0
     for (int k = tid; k < p0; k += blockDim.x) {
-      T acc = T(0);
+      T acc[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) acc[v] = T(0);
       for (int j = 0; j < np; j++) {
         long long row = b0 + p0 + j;
-        acc = fma(L[row * (row + 1) / 2 + b0 + k], y2[p0 + j], acc);
+        const T lv = L[row * (row + 1) / 2 + b0 + k];
+#pragma unroll
+        for (int v = 0; v < NV; v++) acc[v] = fma(lv, y[v * nb + b0 + p0 + j], acc[v]);
       }
-      y2[k] -= acc;
+#pragma unroll
+      for (int v = 0; v < NV; v++) y[v * nb + b0 + k] -= acc[v];
     }
     __syncthreads();
   }
   if (full) {
     double* Yc = Y + boff[c];
-    for (int j = tid; j < nb; j += blockDim.x) Yc[j < n1 ? nc + j : j - n1] = (double)y[j];
+    for (int j = tid; j < nb; j += blockDim.x)
+#pragma unroll
+      for (int v = 0; v < NV; v++) Yc[v * ys + (j < n1 ? nc + j : j - n1)] = (double)y[v * nb + j];
   } else {
-    for (int i = tid; i < nc; i += blockDim.x) out[cs[c] + i] = (double)y2[i];
+    for (int i = tid; i < nc; i += blockDim.x)
+#pragma unroll
+      for (int v = 0; v < NV; v++) out[v * vs + cs[c] + i] = (double)y[v * nb + n1 + i];
   }
 }
 
 // basic Schwarz: out[i] = sum of the slots of point i (ascending slot = ascending block)
-__global__ void k_asm_gather(int n, const long long* __restrict__ inv_off, const long long* __restrict__ inv_slot,
-                             const double* __restrict__ Y, double* __restrict__ out, const int* __restrict__ skip) {
+__global__ void k_asm_gather(int n, int nv, const long long* __restrict__ inv_off,
+                             const long long* __restrict__ inv_slot, const double* __restrict__ Y, long long ys,
+                             double* __restrict__ out, long long vs, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (long long k = inv_off[i]; k < inv_off[i + 1]; k++) s += Y[inv_slot[k]];
-    out[i] = s;
-  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int v = 0; v < nv; v++) {
+      double s = 0.0;
+      for (long long k = inv_off[i]; k < inv_off[i + 1]; k++) s += Y[v * ys + inv_slot[k]];
+      out[v * vs + i] = s;
+    }
 }
 
 // inverse of the buffer lists: per point, the slots that hold it
@@ -765,6 +809,9 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   const int ncell = G.ncell;
   R.fp32 = fp32;
   R.ncell = ncell;
+  // several right-hand sides per launch pay off in FP32 (the factor read is shared); the
+  // FP64 solves are bound by the FP64 pipe and lose occupancy with more vectors
+  if (!fp32) R.max_nv = 1;
   // host plan: offsets of S_c, the list of non-empty blocks (largest first, so the batches
   // of the factorisation keep similar sizes together and the long blocks start early)
   std::vector<long long> hso(ncell + 1);
@@ -794,7 +841,8 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
     // slots of each point (deterministic summation of the block solutions)
     long long nslot = 0;
     for (int c = 0; c < ncell; c++) nslot += hcnt[c];
-    R.Y.reserve(std::max<long long>(nslot, 1));
+    R.nslot = nslot;
+    R.Y.reserve(std::max<long long>(nslot, 1) * std::max(1, std::min(4, R.max_nv)));
     R.inv_off.reserve((size_t)G.n + 1);
     R.inv_slot.reserve(std::max<long long>(nslot, 1));
     long long* cur = (long long*)ws.get(47, sizeof(long long) * ((size_t)G.n + 1));
@@ -906,37 +954,87 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   }
 }
 
-void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s, const int* skip) {
-  if (R.nblocks == 0) return;
-  size_t sm = (size_t)R.max_nb * (R.fp32 ? sizeof(float) : sizeof(double));
+namespace {
+template <class T>
+void apply_tri_nv(const RasmPlan& R, const T* Lp, const int* cs, const double* r, double* out, long long vs, int nv,
+                  cudaStream_t s, const int* skip) {
+  const size_t sm = (size_t)nv * R.max_nb * sizeof(T);
   const int full = R.basic ? 1 : 0;
-  if (R.factor && !R.fp32)
-    k_apply_tri<double><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L64.get(), r,
-                                                 out, skip, full, R.Y.get(), R.seg);
-  else if (R.factor)
-    k_apply_tri<float><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), R.L32.get(), r,
-                                                out, skip, full, R.Y.get(), R.seg);
-  else
-    k_apply<float><<<R.ncell, 128, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.soff.get(), R.S32.get(), r, out,
-                                            skip);
+  switch (nv) {
+    case 1:
+      k_apply_tri<T, 1><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
+                                                 skip, full, R.Y.get(), R.nslot, R.seg);
+      break;
+    case 2:
+      k_apply_tri<T, 2><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
+                                                 skip, full, R.Y.get(), R.nslot, R.seg);
+      break;
+    case 3:
+      k_apply_tri<T, 3><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
+                                                 skip, full, R.Y.get(), R.nslot, R.seg);
+      break;
+    default:
+      k_apply_tri<T, 4><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
+                                                 skip, full, R.Y.get(), R.nslot, R.seg);
+      break;
+  }
   PRBF_CHECK_LAUNCH();
-  if (R.basic) {
-    k_asm_gather<<<ceil_div(R.n, 256), 256, 0, s>>>(R.n, R.inv_off.get(), R.inv_slot.get(), R.Y.get(), out, skip);
-    PRBF_CHECK_LAUNCH();
+}
+
+template <class T>
+void set_tri_smem(const RasmPlan& R) {
+  const size_t st = sizeof(T) * 32 * 33;
+  for (int nv = 1; nv <= std::max(1, std::min(4, R.max_nv)); nv++) {
+    size_t sm = (size_t)nv * std::max(R.max_nb, 1) * sizeof(T);
+    if (sm + st > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
+    const void* f = nv == 1 ? (const void*)k_apply_tri<T, 1>
+                            : nv == 2 ? (const void*)k_apply_tri<T, 2>
+                                      : nv == 3 ? (const void*)k_apply_tri<T, 3> : (const void*)k_apply_tri<T, 4>;
+    PRBF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  }
+}
+}  // namespace
+
+void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s, const int* skip, int nv,
+                long long vstride) {
+  if (R.nblocks == 0 || nv <= 0) return;
+  const int step = std::max(1, std::min(4, R.max_nv));
+  for (int v0 = 0; v0 < nv; v0 += step) {
+    const int k = std::min(step, nv - v0);
+    const double* rv = r + v0 * vstride;
+    double* ov = out + v0 * vstride;
+    if (R.factor) {
+      if (R.fp32)
+        apply_tri_nv<float>(R, R.L32.get(), cs, rv, ov, vstride, k, s, skip);
+      else
+        apply_tri_nv<double>(R, R.L64.get(), cs, rv, ov, vstride, k, s, skip);
+    } else {
+      for (int v = 0; v < k; v++) {
+        const size_t sm = (size_t)R.max_nb * sizeof(float);
+        k_apply<float><<<R.ncell, 128, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.soff.get(), R.S32.get(),
+                                                rv + v * vstride, ov + v * vstride, skip);
+        PRBF_CHECK_LAUNCH();
+      }
+    }
+    if (R.basic) {
+      k_asm_gather<<<ceil_div(R.n, 256), 256, 0, s>>>(R.n, k, R.inv_off.get(), R.inv_slot.get(), R.Y.get(), R.nslot,
+                                                      ov, vstride, skip);
+      PRBF_CHECK_LAUNCH();
+    }
   }
 }
 
 void rasm_set_apply_smem(const RasmPlan& R) {
-  // dynamic: the block's right-hand side; static: k_apply_tri's 32 x 33 triangle tile
-  size_t sm = (size_t)std::max(R.max_nb, 1) * (R.fp32 ? sizeof(float) : sizeof(double));
-  size_t st = R.factor ? (R.fp32 ? sizeof(float) : sizeof(double)) * 32 * 33 : 0;
-  if (sm + st > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
-  if (R.factor && !R.fp32)
-    PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  else if (R.factor)
-    PRBF_CUDA(cudaFuncSetAttribute(k_apply_tri<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  else
+  if (R.factor) {
+    if (R.fp32)
+      set_tri_smem<float>(R);
+    else
+      set_tri_smem<double>(R);
+  } else {
+    size_t sm = (size_t)std::max(R.max_nb, 1) * sizeof(float);
+    if (sm > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
     PRBF_CUDA(cudaFuncSetAttribute(k_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  }
 }
 
 }  // namespace prbf

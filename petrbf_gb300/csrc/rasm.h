@@ -25,6 +25,8 @@ struct RasmPlan {
   DevBuf<long long> inv_off;  // basic form: per point, its slots (n + 1 offsets)
   DevBuf<long long> inv_slot; // basic form: the slots, ascending
   SegSkip seg;                // batches: skip the blocks of stopped problems (when seg.done set)
+  int max_nv = 1;             // right-hand sides per apply launch (1..4; set before the build)
+  long long nslot = 0;        // basic form: buffer-list entries (slot stride of Y)
 };
 
 // Buffer lists, blocks, factorisations and S_c for every non-empty cell of P.
@@ -55,7 +57,9 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
 void rasm_set_apply_smem(const RasmPlan& R);
 // Restricted: out[centre(c)] = (A_c^-1 r[buffer(c)])[centre] for every cell; basic:
 // out = sum_c R_c^T A_c^-1 R_c r (sorted order, n entries).
+// nv vectors at stride vstride (applied up to min(4, R.max_nv) at a time; the factor is
+// read once per launch for all of them).
 void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, cudaStream_t s,
-                const int* skip = nullptr);
+                const int* skip = nullptr, int nv = 1, long long vstride = 0);
 
 }  // namespace prbf

@@ -36,7 +36,7 @@ struct GaussRasmOp : Operator {
     gauss_sum_dev(*plan, v, v, x, y, fp32, err, s, skip, nv, vstride);
   }
   void apply_B(const double* r, double* z, const int* skip, cudaStream_t s) const override {
-    for (int k = 0; k < nv; k++) rasm_apply(*rasm, v.cell_start, r + k * vstride, z + k * vstride, s, skip);
+    rasm_apply(*rasm, v.cell_start, r, z, s, skip, nv, vstride);
   }
 };
 
@@ -100,6 +100,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   double budget = std::min(16.0e9, 0.25 * (double)free_b);
   // FP32 blocks: S_c (one GEMV per apply) in 2D; in 3D the blocks are too ill-conditioned
   // for an explicit FP32 inverse, so the FP32 factor is kept and applied by substitution
+  S.rasm.max_nv = std::min(4, nrhs);
   rasm_build(S.rasm, S.pts, mixed, c.ws, c.err.get(), c.stream, budget, mixed && dim == 3,
              p.pc_type == PRBF_PC_ASM);
   rasm_set_apply_smem(S.rasm);
