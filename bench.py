@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--m3", type=int, default=128, help="3D lattice edge (vortex3d)")
     ap.add_argument("--nprob", type=int, default=256, help="problems (batch2d)")
     ap.add_argument("--batch-max-it", type=int, default=1000)
+    ap.add_argument("--case", default=None, help="run one small kernel case (ncu captures) and exit")
     return ap.parse_args()
 
 
@@ -422,8 +423,59 @@ def run_batch2d(args, rank):
                                     matvec_gpairs_per_s_in_solve=None)}), flush=True)
 
 
+def run_case(name):
+    """Small single-kernel cases for ncu captures (a few GB on the device at most)."""
+    import torch
+    from petrbf_gb300 import workloads as W
+    from petrbf_gb300.api import Context, batch_interpolate
+    if name in ("gauss32_2d", "gauss64_2d"):  # 10^6-point jittered lattice, config-2 geometry
+        x, y, h = W.lattice_2d(1000, jitter=0.25, seed=1)
+        c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
+        c.matvec_setup(x, y)
+        v = torch.randn(len(x), dtype=torch.float64, device="cuda")
+        o = torch.empty_like(v)
+        torch.cuda.synchronize()
+        for _ in range(3):
+            c.matvec_dev(v.data_ptr(), o.data_ptr(), cell_order=True, fp32=(name == "gauss32_2d"))
+        c.synchronize()
+    elif name in ("gauss32_3d", "gauss64_3d"):  # 48^3 jittered lattice, config-3 geometry
+        x, y, z, h = W.lattice_3d(48, jitter=0.25, seed=1)
+        c = Context(dim=3, sigma=h / 0.8, nsigma_box=2, sigma_buffer=6, sigma_trunc=16)
+        c.matvec_setup(x, y, z)
+        v = torch.randn(len(x), dtype=torch.float64, device="cuda")
+        o = torch.empty_like(v)
+        torch.cuda.synchronize()
+        for _ in range(3):
+            c.matvec_dev(v.data_ptr(), o.data_ptr(), cell_order=True, fp32=(name == "gauss32_3d"))
+        c.synchronize()
+    elif name == "asm32_3d":  # FP32 basic-Schwarz blocks of the 48^3 case
+        x, y, z, h = W.lattice_3d(48, jitter=0.25, seed=1)
+        c = Context(dim=3, sigma=h / 0.8, nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="asm")
+        c.matvec_setup(x, y, z)
+        c.pc_setup("mixed")
+        r = np.random.default_rng(1).standard_normal(len(x))
+        for _ in range(3):
+            c.pc_apply(r)
+    elif name == "chol64_2d":  # FP64 block factorisation, 400^2 jittered lattice, config-2 blocks
+        x, y, h = W.lattice_2d(400, jitter=0.25, seed=1)
+        c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
+        c.matvec_setup(x, y)
+        c.pc_setup("fp64")
+        r = np.random.default_rng(1).standard_normal(len(x))
+        for _ in range(3):
+            c.pc_apply(r)
+    elif name == "batch":  # 24 problems of the batched form (N up to 6x10^4)
+        batch_interpolate(W.config4(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
+    else:
+        raise SystemExit("unknown case " + name)
+    print("case", name, "done")
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case)
+        return
     rank, world = dist_init(args.gpus)
     if args.workload == "vortex3d":
         if rank == 0:

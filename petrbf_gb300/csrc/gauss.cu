@@ -131,7 +131,6 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   __shared__ int s_fill[3];  // npieces, valid total, done flag
   __shared__ int s_cursor[2];
   __shared__ int s_abort;
-  __shared__ int s_ra[kMaxRanges], s_rb[kMaxRanges];  // source ranges of the item's columns
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   if (!F32)
@@ -170,12 +169,6 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
     const int nranges = ncolx * (jz1 - jz0 + 1);
 
     __syncthreads();  // the previous item's readers of tgt/acc/comp are done
-    // the column ranges, loaded by all threads at once (thread 0 plans the fills from them)
-    for (int r = tid; r < min(nranges, kMaxRanges); r += kThreads) {
-      const int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
-      s_ra[r] = cs_s[cb + cell_of(g, jx, jy0, jz)];
-      s_rb[r] = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
-    }
     for (int t = tid; t < nt; t += kThreads) {
       tgt[t] = (T)((tx[t0 + t] - xc) * scale);
       tgt[kTileT + t] = (T)((ty[t0 + t] - yc) * scale);
@@ -268,14 +261,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
         unsigned bytes = 0;
         while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
           int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
-          int a, b;
-          if (r < kMaxRanges) {
-            a = s_ra[r];
-            b = s_rb[r];
-          } else {
-            a = cs_s[cb + cell_of(g, jx, jy0, jz)];
-            b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
-          }
+          // (the FP64 kernel keeps no range table: with three weight vectors two CTAs per SM
+          // fill the shared memory to within a few hundred bytes)
+          int a = cs_s[cb + cell_of(g, jx, jy0, jz)], b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
           int s = p < 0 ? a : p;
           if (s >= b) {
             r++;
