@@ -76,6 +76,14 @@ def allmax(v, world):
     return float(t.item())
 
 
+def replica_value(units_per_step, steps, ms_local, world):
+    """Whole-job throughput of N independent replicas: every rank processed the same units
+    per step; the job's time is the slowest rank's (max over ranks). Returns (Gunits/s,
+    max ms)."""
+    ms = allmax(ms_local, world)
+    return units_per_step * steps * world / (ms * 1e-3) / 1e9, ms
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -262,8 +270,7 @@ def run_ours(args, rank, world):
         barrier(world)
         t_wall = time.perf_counter() - t_wall0
     ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-    ms = allmax(ms, world)
-    value = pairs * args.steps * world / (ms * 1e-3) / 1e9
+    value, ms = replica_value(pairs, args.steps, ms, world)
     # ---- end to end through the C ABI with pinned host vectors ----------------------------------
     hin = torch.randn(n, dtype=torch.float64).pin_memory()
     hout = torch.empty(n, dtype=torch.float64).pin_memory()

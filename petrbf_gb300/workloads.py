@@ -150,6 +150,29 @@ def config4(nprob=256, seed=2024, nmin=2000, nmax=200000, nsigma_box=4):
     return out
 
 
+def read_cdata(path):
+    """A scattered-data file in the reference's cdata format: whitespace-separated records
+    of four numbers per particle, x y g e (read in that order by 2d/cylinder.cxx:82-90;
+    line breaks anywhere). Returns (x, y, g, e) as FP64 arrays."""
+    with open(path) as fh:
+        v = np.array(fh.read().split(), dtype=np.float64)
+    if v.size == 0 or v.size % 4:
+        raise ValueError("cdata: expected records of 4 numbers, got %d numbers" % v.size)
+    v = v.reshape(-1, 4)
+    return (v[:, 0].copy(), v[:, 1].copy(), v[:, 2].copy(), v[:, 3].copy())
+
+
+def cylinder_problem(x, y, e, overlap=0.9, nsigma_box=5, buffer_factor=1.9):
+    """The cylinder driver's parameters (2d/cylinder.cxx:43-55, run line 2d/Makefile:18):
+    sigma = 0.007, sigma_buffer = (int)(nsigma_box * 1.9), sigma_trunc = nsigma_box + 4
+    for overlap >= 0.8 + epsf (else + 6); the right-hand side is the e column."""
+    sigma = 0.007
+    sigma_buffer = int(nsigma_box * buffer_factor)
+    sigma_trunc = nsigma_box + (6 if overlap < 0.8 + 1e-6 else 4)
+    return Problem("2d_cylinder_cdata", x, y, None, e.copy(), sigma, nsigma_box, sigma_buffer, sigma_trunc,
+                   exact=e, meta={"overlap": overlap})
+
+
 def log10_rel_error(w, e):
     """log10(||w - e||_2 / ||e||_2), 2d/main.cxx:130-133."""
     w = np.asarray(w, np.float64)

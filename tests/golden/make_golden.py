@@ -94,6 +94,20 @@ def main(ref_root):
     x, y, z, h = W.lattice_3d(16, jitter=0.25, seed=424242)
     _case("g3d_jitter16", 3, x, y, z, h / 0.8, 4, 6, 6, blocks=(0, 17),
           eval_targets=(x[::7] + 0.3 * h, y[::7] - 0.2 * h, z[::7] + 0.1 * h))
+    # 5. the reference's own scattered-data fixture (2d/cdata, 5346 particles around a
+    #    cylinder) with the cylinder driver's parameters (2d/cylinder.cxx:43-55,
+    #    2d/Makefile:18); the oracle's solve of it (weights, iterations, error) is stored too
+    x, y, g, e = W.read_cdata(os.path.join(ref_root, "2d", "cdata"))
+    p = W.cylinder_problem(x, y, e)
+    _case("g2d_cdata", 2, x, y, None, *p.params(), blocks=tuple(range(0, 1089, 97)))  # empty cells dropped
+    gw, its, reason = O.rbf_interpolation(x, y, None, e, *p.params(), rtol=1e-13, max_it=1000)
+    w = O.vorticity_evaluation(x, y, None, x, y, None, gw, *p.params())
+    path = os.path.join(HERE, "g2d_cdata.npz")
+    d = dict(np.load(path))
+    d.update(cdata_g=g, cdata_e=e, solve_weights=gw, solve_its=np.array([its]), solve_reason=np.array([reason]),
+             solve_log10_err=np.array([W.log10_rel_error(w, e)]))
+    np.savez_compressed(path, **d)
+    print("cdata: its %d reason %d log10 err %.4f" % (its, reason, d["solve_log10_err"][0]))
 
 
 if __name__ == "__main__":

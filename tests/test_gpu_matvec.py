@@ -10,7 +10,7 @@ from petrbf_gb300.api import Context, PrbfError
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["g2d_lattice100", "g2d_jitter48", "g2d_ragged", "g3d_jitter16"]
+CASES = ["g2d_lattice100", "g2d_jitter48", "g2d_ragged", "g3d_jitter16", "g2d_cdata"]
 RTOL_FP64 = 1e-12  # plain FP64 matvec vs the reference, relative 2-norm
 RTOL_FP32 = 2e-5   # FP32 pair arithmetic (mixed-precision inner matvec)
 

@@ -264,3 +264,18 @@ def test_solve_errors():
         with pytest.raises(PrbfError) as e:
             c.interpolate(p.x, p.y, None, bad)
         assert e.value.status == 7  # PRBF_ERR_NAN
+
+
+def test_cdata_cylinder_matches_oracle(golden):
+    # the reference's scattered-data fixture (2d/cdata) with the cylinder driver's
+    # parameters: the GPU solve against the oracle's stored solve
+    d = golden("g2d_cdata")
+    p = W.cylinder_problem(d["x"], d["y"], d["cdata_e"])
+    with _ctx(p, rtol=1e-13, max_it=1000) as c:
+        g, st = c.interpolate(p.x, p.y, None, p.f)
+        w = c.evaluate(p.x, p.y, None, p.x, p.y, None, g)
+    assert st.reason == 2 and abs(st.its - int(d["solve_its"][0])) <= 2
+    assert _rel(g, d["solve_weights"]) <= RTOL_WEIGHTS_AT_1E13
+    # error metric of the cylinder driver (2d/cylinder.cxx:123-127): residual level
+    err = W.log10_rel_error(w, p.f)
+    assert err < -13.0 and abs(err - float(d["solve_log10_err"][0])) < 0.5

@@ -7,7 +7,7 @@ import scipy.linalg as sla
 import oracle as O
 from petrbf_gb300 import workloads as W
 
-CASES = ["g2d_lattice100", "g2d_jitter48", "g2d_ragged", "g3d_jitter16"]
+CASES = ["g2d_lattice100", "g2d_jitter48", "g2d_ragged", "g3d_jitter16", "g2d_cdata"]
 
 
 def _setup(d):
@@ -168,3 +168,30 @@ def test_rbf_interpolation_config1_error():
     w = O.vorticity_evaluation(p.x, p.y, None, p.x, p.y, None, gw, *p.params())
     err = W.log10_rel_error(w, p.exact)
     assert err < -11.0
+
+
+def test_cdata_reader_roundtrip(tmp_path, golden):
+    # the reference's scattered-data format: 4 numbers per particle, any line breaks
+    d = golden("g2d_cdata")
+    x, y, g, e = d["x"], d["y"], d["cdata_g"], d["cdata_e"]
+    rec = np.stack([x, y, g, e], axis=1).ravel()
+    text = " ".join("%.17g" % v for v in rec[:101]) + "\n" + "\n".join("%.17g" % v for v in rec[101:])
+    (tmp_path / "cdata").write_text(text)
+    xr, yr, gr, er = W.read_cdata(str(tmp_path / "cdata"))
+    for a, b in ((xr, x), (yr, y), (gr, g), (er, e)):
+        np.testing.assert_array_equal(a, b)
+    (tmp_path / "bad").write_text("1 2 3")
+    with pytest.raises(ValueError):
+        W.read_cdata(str(tmp_path / "bad"))
+
+
+def test_cdata_cylinder_solve_reproduces_fixture(golden):
+    # the cylinder driver on the reference's own data (2d/cylinder.cxx:43-55, 118-127)
+    d = golden("g2d_cdata")
+    p = W.cylinder_problem(d["x"], d["y"], d["cdata_e"])
+    assert p.params() == (0.007, 5, 9, 9)
+    gw, its, reason = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), rtol=1e-13, max_it=1000)
+    assert reason == 2 and its == int(d["solve_its"][0])
+    np.testing.assert_allclose(gw, d["solve_weights"], rtol=0, atol=1e-12 * np.abs(d["solve_weights"]).max())
+    w = O.vorticity_evaluation(p.x, p.y, None, p.x, p.y, None, gw, *p.params())
+    assert abs(W.log10_rel_error(w, p.f) - float(d["solve_log10_err"][0])) < 1e-6
