@@ -40,12 +40,23 @@ constexpr int kRawCap = 1024;  // staged raw sources per fill (incl. alignment p
 constexpr int kMaxPieces = 64; // source ranges per fill
 constexpr int kMaxRanges = 256; // column ranges of an item kept in shared memory
 
-// exp table: e^a with a = -L*d, d >= 0, L = ln2/kTab:  k = rint(d), r = k - d in [-1/2, 1/2],
-// e^a = 2^(-k/kTab) e^(L r) = 2^-m T[j] sum_i (L r)^i / i!,  k = m*kTab + j.
-constexpr int kTabBits = 8;
-constexpr int kTab = 1 << kTabBits;
-constexpr int kPoly = 5;  // degree-4 polynomial, coefficients T[j] L^i / i!
-__device__ double d_tab[kPoly][kTab];  // copied into shared memory by each CTA
+// exp table: e^a with a = -L*d, d >= 0, L = ln2/n:  k = rint(d), r = k - d in [-1/2, 1/2],
+// e^a = 2^(-k/n) e^(L r) = 2^-m T[j] p(r),  k = m*n + j; the table holds T[j] c_i
+// interleaved per j. Large table: n = 1024 and the cubic interpolating e^(L r) at the 4
+// Chebyshev nodes of [-1/2, 1/2] (near-minimax, |p - e^(Lr)| / e^(Lr) <= 2 (L/4)^4 / 4! ~
+// 7e-17): 11 FP64 instructions per 2D pair. Small table: n = 256 and the quartic Taylor
+// polynomial (remainder (L/2)^5 / 5! ~ 4e-17), for the kernels whose shared memory would
+// otherwise drop to one CTA per SM (3D, and 2D with more than two weight vectors).
+template <bool BIG>
+struct ExpTab {
+  static constexpr int bits = BIG ? 10 : 8, n = 1 << bits, poly = BIG ? 4 : 5;
+};
+template <int DIM, int NV>
+struct UseBigTab {
+  static constexpr bool v = DIM == 2 && NV <= 2;
+};
+__device__ double d_tab_big[ExpTab<true>::n * ExpTab<true>::poly];  // copied into shared memory by each CTA
+__device__ double d_tab_small[ExpTab<false>::n * ExpTab<false>::poly];
 
 template <int DIM, bool F32, int NV>
 struct Cfg {
@@ -71,7 +82,8 @@ struct Layout {
   static constexpr size_t tgt = align16(comp + sizeof(T) * NA * Cfg<DIM, F32, NV>::kComp);
   static constexpr size_t acc = align16(tgt + sizeof(T) * DIM * kTileT);
   static constexpr size_t tab = align16(acc + sizeof(T) * NV * kTileT);
-  static constexpr size_t pieces = align16(tab + (F32 ? 0 : sizeof(double) * kPoly * kTab));
+  using ET = ExpTab<UseBigTab<DIM, NV>::v>;
+  static constexpr size_t pieces = align16(tab + (F32 ? 0 : sizeof(double) * ET::poly * ET::n));
   static constexpr size_t bar = align16(pieces + sizeof(Piece) * kMaxPieces);
   static constexpr size_t total = bar + 16;
 };
@@ -94,11 +106,11 @@ struct SumConsts {
   double scale, kexp, norm;
 };
 
-__host__ __device__ inline SumConsts sum_consts(double sigma, bool f32) {
+__host__ __device__ inline SumConsts sum_consts(double sigma, bool f32, int ntab) {
   const double ln2 = 0.6931471805599453;  // ln 2 rounded to double
   SumConsts k;
   k.scale = f32 ? sqrt(1.0 / (2.0 * sigma * sigma * ln2)) : 1.0;
-  k.kexp = (double)kTab / (2.0 * sigma * sigma * ln2);
+  k.kexp = (double)ntab / (2.0 * sigma * sigma * ln2);
   k.norm = 1.0 / (2 * 3.141592653589793 * sigma * sigma);
   return k;
 }
@@ -124,7 +136,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   T* comp = (T*)(smem + lay.comp);              // NA x kComp (compacted truncation set)
   T* tgt = (T*)(smem + lay.tgt);                // DIM x kTileT
   T* acc = (T*)(smem + lay.acc);                // NV x kTileT
-  double* tab = (double*)(smem + lay.tab);      // kPoly x kTab (FP64 form only)
+  double* tab = (double*)(smem + lay.tab);      // exp table (FP64 form only)
+  using ET = ExpTab<UseBigTab<DIM, NV>::v>;
   Piece* pieces = (Piece*)(smem + lay.pieces);  // kMaxPieces
   uint64_t* bar = (uint64_t*)(smem + lay.bar);
   __shared__ int s_wsum[kWarps];
@@ -134,7 +147,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   if (!F32)
-    for (int i = tid; i < kPoly * kTab; i += kThreads) tab[i] = (&d_tab[0][0])[i];
+    for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (UseBigTab<DIM, NV>::v ? d_tab_big : d_tab_small)[i];
   if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
   const int G = gridDim.x;
@@ -149,7 +162,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
     if constexpr (BATCH) {
       if (seg.cell_done(ic)) continue;  // a stopped problem (uniform over the CTA)
       g = grids[cprob[ic]];
-      kc = sum_consts(g.sigma, F32);
+      kc = sum_consts(g.sigma, F32, ET::n);
     }
     const double scale = kc.scale, kexp = kc.kexp;
     const int cb = g.cbase;
@@ -221,20 +234,29 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
               for (int v = 0; v < NV; v++) a[k][v] = fmaf(sgj[v], e, a[k][v]);
             } else {
               // d2 = |x_t - x_s|^2 (unscaled: the differences are exact as in the reference);
-              // in units of L = ln2/kTab the exponent is kexp*d2, kexp = kTab/(2 sigma^2 ln2):
+              // in units of L = ln2/n the exponent is kexp*d2, kexp = n/(2 sigma^2 ln2):
               // k = rint(kexp d2) (fused), r = k - kexp d2 in [-1/2, 1/2] with a single rounding
               const double magic = 6755399441055744.0;  // 1.5 * 2^52
               double kd = fma(d2, kexp, magic);
               int kk = __double2loint(kd);
               double r = fma(-d2, kexp, kd - magic);
-              int j8 = kk & (kTab - 1);
+              int j8 = kk & (ET::n - 1);
               // m <= 900 keeps every scaled coefficient normal (2^-900 ~ 1e-271)
-              int m20 = min(kk >> kTabBits, 900) << 20;
-              double q = hi_sub(tab[4 * kTab + j8], m20);
-              q = fma(r, q, hi_sub(tab[3 * kTab + j8], m20));
-              q = fma(r, q, hi_sub(tab[2 * kTab + j8], m20));
-              q = fma(r, q, hi_sub(tab[1 * kTab + j8], m20));
-              q = fma(r, q, hi_sub(tab[j8], m20));
+              int m20 = min(kk >> ET::bits, 900) << 20;
+              double q;
+              if constexpr (ET::poly == 4) {
+                const double2 c01 = *(const double2*)(tab + 4 * j8);
+                const double2 c23 = *(const double2*)(tab + 4 * j8 + 2);
+                q = hi_sub(c23.y, m20);
+                q = fma(r, q, hi_sub(c23.x, m20));
+                q = fma(r, q, hi_sub(c01.y, m20));
+                q = fma(r, q, hi_sub(c01.x, m20));
+              } else {
+                const double* cj = tab + ET::poly * j8;
+                q = hi_sub(cj[ET::poly - 1], m20);
+#pragma unroll
+                for (int i = ET::poly - 2; i >= 0; i--) q = fma(r, q, hi_sub(cj[i], m20));
+              }
 #pragma unroll
               for (int v = 0; v < NV; v++) a[k][v] = fma(sgj[v], q, a[k][v]);
             }
@@ -751,19 +773,46 @@ void upload_table(cudaStream_t s) {
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && g_tab_ready[dev]) return;
-  // T[j] = 2^(-j/kTab) in long double, then the folded Taylor coefficients T L^i / i!
-  static double h[kPoly][kTab];
-  const long double L = logl(2.0L) / kTab;
-  for (int j = 0; j < kTab; j++) {
-    long double t = exp2l(-(long double)j / kTab);
-    long double f = 1.0L, lp = 1.0L;
-    for (int i = 0; i < kPoly; i++) {
-      h[i][j] = (double)(t * lp / f);
-      lp *= L;
-      f *= (long double)(i + 1);
+  // Large table: c_i = monomial coefficients of the cubic through (r_k, e^(L r_k)) at the
+  // Chebyshev nodes r_k = cos((2k+1) pi / 8) / 2 (Newton divided differences, then
+  // expanded), in long double; small table: c_i = L^i / i!. Then T[j] = 2^(-j/n) and the
+  // folded coefficients T[j] c_i.
+  static double h2[ExpTab<true>::n * ExpTab<true>::poly], h3[ExpTab<false>::n * ExpTab<false>::poly];
+  const long double PI = 3.141592653589793238462643383279502884L;
+  {
+    constexpr int NP = ExpTab<true>::poly, NT = ExpTab<true>::n;
+    const long double L = logl(2.0L) / NT;
+    long double xr[NP], dd[NP], c[NP];
+    for (int k = 0; k < NP; k++) {
+      xr[k] = 0.5L * cosl((2 * k + 1) * PI / (2 * NP));
+      dd[k] = expl(L * xr[k]);
+      c[k] = 0.0L;
+    }
+    for (int lev = 1; lev < NP; lev++)
+      for (int k = NP - 1; k >= lev; k--) dd[k] = (dd[k] - dd[k - 1]) / (xr[k] - xr[k - lev]);
+    for (int k = NP - 1; k >= 0; k--) {  // Newton form -> monomials (Horner)
+      for (int i = NP - 1; i > 0; i--) c[i] = c[i - 1] - xr[k] * c[i];
+      c[0] = dd[k] - xr[k] * c[0];
+    }
+    for (int j = 0; j < NT; j++) {
+      long double t = exp2l(-(long double)j / NT);
+      for (int i = 0; i < NP; i++) h2[j * NP + i] = (double)(t * c[i]);
     }
   }
-  PRBF_CUDA(cudaMemcpyToSymbolAsync(d_tab, h, sizeof(h), 0, cudaMemcpyHostToDevice, s));
+  {
+    constexpr int NP = ExpTab<false>::poly, NT = ExpTab<false>::n;
+    const long double L = logl(2.0L) / NT;
+    for (int j = 0; j < NT; j++) {
+      long double t = exp2l(-(long double)j / NT), f = 1.0L, lp = 1.0L;
+      for (int i = 0; i < NP; i++) {
+        h3[j * NP + i] = (double)(t * lp / f);
+        lp *= L;
+        f *= (long double)(i + 1);
+      }
+    }
+  }
+  PRBF_CUDA(cudaMemcpyToSymbolAsync(d_tab_big, h2, sizeof(h2), 0, cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyToSymbolAsync(d_tab_small, h3, sizeof(h3), 0, cudaMemcpyHostToDevice, s));
   PRBF_CUDA(cudaStreamSynchronize(s));
   if (dev < 64) g_tab_ready[dev] = true;
 }
@@ -787,9 +836,9 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
     if (dev < 64) attr_set[dev] = true;
   }
   // FP32: coordinates scaled so that |dx|^2 is the exponent in units of ln2 (exp2).
-  // FP64: unscaled cell-relative coordinates; kexp = kTab / (2 sigma^2 ln2) converts |dx|^2
-  // to units of ln2/kTab inside the fused range reduction.
-  const SumConsts k0 = sum_consts(P.g.sigma, F32);
+  // FP64: unscaled cell-relative coordinates; kexp = n / (2 sigma^2 ln2) converts |dx|^2
+  // to units of ln2/n (n the exp table size) inside the fused range reduction.
+  const SumConsts k0 = sum_consts(P.g.sigma, F32, ExpTab<UseBigTab<DIM, NV>::v>::n);
   const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
   k_gauss<DIM, F32, NV, BATCH><<<grid, kThreads, sm, st>>>(P.g, P.grids.get(), P.cprob.get(), P.items.get(), P.nitems,
                                                            t.x, t.y, t.z, t.cell_start, s.x, s.y, s.z, gv,
@@ -809,7 +858,7 @@ void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, c
     PRBF_CUDA(cudaFuncSetAttribute(k_gauss_f32m<DIM, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
-  const SumConsts k0 = sum_consts(P.g.sigma, true);
+  const SumConsts k0 = sum_consts(P.g.sigma, true, 0);
   k_to_f32<<<4 * 152, 256, 0, st>>>(s.n, NV, vstride, P.g32_stride, gv, P.g32.get(), skip);
   PRBF_CHECK_LAUNCH();
   const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
@@ -902,7 +951,7 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
     for (auto* b : {&plan.su, &plan.sv}) PRBF_CUDA(cudaMemsetAsync(b->get(), 0, sizeof(float) * n8, s));
     if (g.dim == 3) PRBF_CUDA(cudaMemsetAsync(plan.sw.get(), 0, sizeof(float) * n8, s));
     PRBF_CUDA(cudaMemsetAsync(plan.smask.get(), 0, sizeof(unsigned long long) * n8, s));
-    const SumConsts k32 = sum_consts(g.sigma, true);
+    const SumConsts k32 = sum_consts(g.sigma, true, 0);
     k_src_f32<<<ceil_div(g.ncell, 128), 128, 0, s>>>(g, src.cell_start, src.x, src.y, src.z, k32.scale,
                                                      plan.su.get(), plan.sv.get(), plan.sw.get(), plan.smask.get());
     PRBF_CHECK_LAUNCH();
