@@ -449,13 +449,18 @@ __global__ void k_to_f32(int n, int nv, long long vs_in, long long vs_out, const
       out[v * vs_out + i] = (float)in[v * vs_in + i];
 }
 
+// The FP32 items are latency-bound on the fills (3D: 16 targets of a 2-sigma cell):
+// smaller fills and compaction buffers let more CTAs share an SM (sizes timed on GB300:
+// 3D 384/768 and 2D 512/1024 beat 1024/2048 by 9 % and 6 %).
 template <int DIM, int NV>
 struct LayoutF {
   static constexpr int NF = DIM + NV;  // FP32 staged arrays: coordinates + weights
-  static constexpr int kComp = 2048;
+  static constexpr int RC = DIM == 3 ? 384 : 512;      // staged sources per fill
+  static constexpr int kComp = DIM == 3 ? 768 : 1024;  // compacted sources (>= RC)
+  static_assert(kComp >= RC, "a fill must fit the compaction buffer");
   static constexpr size_t rawf = 0;
-  static constexpr size_t rawm = align16(rawf + sizeof(float) * NF * kRawCap);
-  static constexpr size_t comp = align16(rawm + sizeof(unsigned long long) * kRawCap);
+  static constexpr size_t rawm = align16(rawf + sizeof(float) * NF * RC);
+  static constexpr size_t comp = align16(rawm + sizeof(unsigned long long) * RC);
   static constexpr size_t tgt = align16(comp + sizeof(float) * NF * kComp);
   static constexpr size_t acc = align16(tgt + sizeof(float) * DIM * kTileT);
   static constexpr size_t pieces = align16(acc + sizeof(float) * NV * kTileT);
@@ -472,10 +477,10 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
     long long vs_w, double scale, double norm, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
   using Lay = LayoutF<DIM, NV>;
-  constexpr int NF = Lay::NF, KC = Lay::kComp;
+  constexpr int NF = Lay::NF, KC = Lay::kComp, RC = Lay::RC;
   extern __shared__ __align__(16) unsigned char smem[];
-  float* rawf = (float*)(smem + Lay::rawf);                           // NF x kRawCap
-  unsigned long long* rawm = (unsigned long long*)(smem + Lay::rawm);  // kRawCap
+  float* rawf = (float*)(smem + Lay::rawf);                           // NF x RC
+  unsigned long long* rawm = (unsigned long long*)(smem + Lay::rawm);  // RC
   float* comp = (float*)(smem + Lay::comp);                           // NF x KC
   float* tgt = (float*)(smem + Lay::tgt);                             // DIM x kTileT
   float* acc = (float*)(smem + Lay::acc);                             // NV x kTileT
@@ -583,7 +588,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
         int r = s_cursor[0], p = s_cursor[1];
         int used = 0, np = 0, valid = 0;
         unsigned bytes = 0;
-        while (r < nranges && np < kMaxPieces && kRawCap - used >= kAlignF) {
+        while (r < nranges && np < kMaxPieces && RC - used >= kAlignF) {
           int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
           int a, b;
           if (r < kMaxRanges) {
@@ -600,7 +605,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
             continue;
           }
           int s_al = s & ~(kAlignF - 1);
-          int room = (kRawCap - used) & ~(kAlignF - 1);
+          int room = (RC - used) & ~(kAlignF - 1);
           int e_al = min((b + kAlignF - 1) & ~(kAlignF - 1), s_al + room);
           int e = min(b, e_al);
           pieces[np].raw_off = used + (s - s_al);
@@ -631,10 +636,10 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
             int len = ((s + pieces[q].count + kAlignF - 1) & ~(kAlignF - 1)) - s_al;
             int dst = pieces[q].raw_off - (s - s_al);
             bulk_g2s(rawf + dst, su + s_al, len * 4u, bar);
-            bulk_g2s(rawf + kRawCap + dst, sv + s_al, len * 4u, bar);
-            if (DIM == 3) bulk_g2s(rawf + 2 * kRawCap + dst, sw + s_al, len * 4u, bar);
+            bulk_g2s(rawf + RC + dst, sv + s_al, len * 4u, bar);
+            if (DIM == 3) bulk_g2s(rawf + 2 * RC + dst, sw + s_al, len * 4u, bar);
 #pragma unroll
-            for (int v = 0; v < NV; v++) bulk_g2s(rawf + (DIM + v) * kRawCap + dst, sg + v * vs_g + s_al, len * 4u, bar);
+            for (int v = 0; v < NV; v++) bulk_g2s(rawf + (DIM + v) * RC + dst, sg + v * vs_g + s_al, len * 4u, bar);
             bulk_g2s(rawm + dst, smask + s_al, len * 8u, bar);
           }
         }
@@ -693,10 +698,10 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
             int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
             const int jy = (int)(m >> kMaskCellY);
             comp[pos] = rawf[ro] + offx;
-            comp[KC + pos] = rawf[kRawCap + ro] + (float)(jy - iy) * boxs;
-            if (DIM == 3) comp[2 * KC + pos] = rawf[2 * kRawCap + ro] + offz;
+            comp[KC + pos] = rawf[RC + ro] + (float)(jy - iy) * boxs;
+            if (DIM == 3) comp[2 * KC + pos] = rawf[2 * RC + ro] + offz;
 #pragma unroll
-            for (int v = 0; v < NV; v++) comp[(DIM + v) * KC + pos] = rawf[(DIM + v) * kRawCap + ro];
+            for (int v = 0; v < NV; v++) comp[(DIM + v) * KC + pos] = rawf[(DIM + v) * RC + ro];
           }
           ncomp += tot;
           __syncthreads();

@@ -113,15 +113,19 @@ def config2(m=2000, seed=12345):
     return lamb_oseen_2d(m, jitter=0.25, seed=seed, name="2d_lamb_oseen_N4e6_jitter")
 
 
-def config3(m=128, seed=12345, nsigma_box=2):
+def config3(m=128, seed=12345, nsigma_box=3, sigma_buffer=7):
     """3D vortex ring, N = 128^3 jittered lattice, three right-hand sides; cutoff 7 sigma
-    past the cell edge (sigma_trunc = nsigma_box + 14), one-cell buffer."""
+    past the cell edge (sigma_trunc = nsigma_box + 14). Cell 3 sigma (~53 points) and a
+    7-sigma Schwarz box (2 sigma of overlap on each side, blocks of up to 729 points): on
+    GB300 this solves the 128^3 mixed problem in 7.8 s against 12.5 s for a 2-sigma cell
+    with a 6-sigma box (blocks of up to 512), with fewer iterations (290 vs 316)."""
     x, y, z, h = lattice_3d(m, jitter=0.25, seed=seed)
     wx, wy, wz = vortex_ring(x, y, z)
     f = np.stack([wx, wy, wz], axis=1)
     sigma = h / 0.8
+    sb = sigma_buffer
     return Problem("3d_vortex_ring_N%d" % (m ** 3), x, y, z, f.copy(), sigma, nsigma_box,
-                   3 * nsigma_box, nsigma_box + 14, exact=f,
+                   sb, nsigma_box + 14, exact=f,
                    meta={"m": m, "h": h, "jitter": 0.25, "seed": seed})
 
 
