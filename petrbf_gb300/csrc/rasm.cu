@@ -398,10 +398,13 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
   T* Minv_all = nullptr;  // diagonal inverses live in Xw after X (see xoff layout)
   int c = blk_cell[b];
   const int nb = (int)(boff[c + 1] - boff[c]);
-  const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
-  const int kc1 = (n1 + TB - 1) / TB;           // neighbour tiles
-  const int ntile = kc1 + (nc + TB - 1) / TB;   // all tiles
-  const int nct = ntile - kc1;                  // centre tiles
+  // S_c (mode 0) needs the centre columns on tile boundaries: neighbour tiles, then
+  // centre tiles. The factor form (mode 1) tiles the block uniformly, which wastes less
+  // of the 64 x 64 tile work on small blocks (two partial tiles become one).
+  const int nc = cs[c + 1] - cs[c], n1 = mode == 1 ? nb : nb - nc;
+  const int kc1 = (n1 + TB - 1) / TB;                            // neighbour (or all) tiles
+  const int ntile = kc1 + (mode == 1 ? 0 : (nc + TB - 1) / TB);  // all tiles
+  const int nct = ntile - kc1;                                   // centre tiles
   T* A = K + koff[b];
   T* X = Xw + xoff[b];                   // nb x (nct*TB), row-major
   const long long ldx = (long long)nct * TB;
