@@ -447,7 +447,7 @@ def run_case(name):
         c.synchronize()
     elif name in ("gauss32_3d", "gauss64_3d"):  # 48^3 jittered lattice, config-3 geometry
         x, y, z, h = W.lattice_3d(48, jitter=0.25, seed=1)
-        c = Context(dim=3, sigma=h / 0.8, nsigma_box=2, sigma_buffer=6, sigma_trunc=16)
+        c = Context(dim=3, sigma=h / 0.8, nsigma_box=3, sigma_buffer=7, sigma_trunc=17)
         c.matvec_setup(x, y, z)
         v = torch.randn(len(x), dtype=torch.float64, device="cuda")
         o = torch.empty_like(v)
@@ -457,7 +457,7 @@ def run_case(name):
         c.synchronize()
     elif name == "asm32_3d":  # FP32 basic-Schwarz blocks of the 48^3 case
         x, y, z, h = W.lattice_3d(48, jitter=0.25, seed=1)
-        c = Context(dim=3, sigma=h / 0.8, nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="asm")
+        c = Context(dim=3, sigma=h / 0.8, nsigma_box=3, sigma_buffer=7, sigma_trunc=17, pc="asm")
         c.matvec_setup(x, y, z)
         c.pc_setup("mixed")
         r = np.random.default_rng(1).standard_normal(len(x))
