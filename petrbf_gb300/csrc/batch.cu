@@ -25,8 +25,6 @@
 
 namespace prbf {
 
-double norm2_host(const double* v, int n, Workspace& ws, cudaStream_t s);
-
 namespace {
 
 double now_ms() {

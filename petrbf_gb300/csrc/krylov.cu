@@ -305,16 +305,6 @@ __global__ void k_axpy(int n, double a, const double* __restrict__ xv, double* _
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) yv[i] = fma(a, xv[i], yv[i]);
 }
 
-__global__ void __launch_bounds__(KT) k_norm2_flat(const double* __restrict__ w, int n, int chunk,
-                                                   double* __restrict__ part) {
-  __shared__ double sh[KT / 32];
-  int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  double s = 0;
-  for (int i = lo + threadIdx.x; i < hi; i += KT) s = fma(w[i], w[i], s);
-  s = block_sum(s, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
 }  // namespace
 
 void Krylov::init(int n_, int m_, cudaStream_t s) { init({0}, {n_}, (long long)n_, m_, s); }
@@ -526,21 +516,6 @@ std::vector<double> seg_norm2_host(const Krylov& K, const double* v, cudaStream_
   PRBF_CUDA(cudaStreamSynchronize(s));
   for (int b = 0; b < K.nblk; b++) out[hb[b]] += hp[b];
   return out;
-}
-
-double norm2_host(const double* v, int n, Workspace& ws, cudaStream_t s) {
-  int chunk = ((n + 303) / 304 + 31) / 32 * 32;
-  chunk = std::max(chunk, 32);
-  int nb = std::max(1, (n + chunk - 1) / chunk);
-  double* part = (double*)ws.get(50, sizeof(double) * nb);
-  k_norm2_flat<<<nb, KT, 0, s>>>(v, n, chunk, part);
-  PRBF_CHECK_LAUNCH();
-  std::vector<double> h(nb);
-  PRBF_CUDA(cudaMemcpyAsync(h.data(), part, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
-  PRBF_CUDA(cudaStreamSynchronize(s));
-  double t = 0;
-  for (double q : h) t += q;
-  return std::sqrt(t);
 }
 
 void axpy_dev(int n, double a, const double* x, double* y, cudaStream_t s) {

@@ -366,6 +366,21 @@ __device__ __forceinline__ void tile_range(int t, int n1, int nb, int kc1, int& 
   }
 }
 
+// Packed factor rows: row i holds L[i][0..i] padded to a multiple of PackA<T> elements
+// (16 bytes), so every row starts 16-byte aligned and 8-element segments at multiples of 8
+// load as vectors. rowoff(i) = sum_{r<i} A ceil((r+1)/A) = A (A q(q+1)/2 + rr (q+1)),
+// q = i / A, rr = i % A.
+template <class T>
+struct PackA {
+  static constexpr int v = 16 / sizeof(T);
+};
+template <class T>
+__host__ __device__ __forceinline__ long long rowoff(long long i) {
+  constexpr long long A = PackA<T>::v;
+  const long long q = i / A, rr = i % A;
+  return A * (A * q * (q + 1) / 2 + rr * (q + 1));
+}
+
 // One CTA per block: Cholesky, centre columns of the inverse, S_c.
 template <class T>
 __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
@@ -453,7 +468,7 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
     const T sc = (T)out_scale;
     // the diagonal is stored as its reciprocal: the substitutions then multiply
     for (int i = 0; i < nb; i++) {
-      long long o = (long long)i * (i + 1) / 2;
+      long long o = rowoff<T>(i);
       for (int j = threadIdx.x; j <= i; j += NTH) {
         T v = A[(long long)i * nb + j] * sc;
         Lp[o + j] = j == i ? T(1) / v : v;
@@ -602,7 +617,7 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     const int np = min(32, nb - p0);
     for (int e = tid; e < 32 * 32; e += blockDim.x) {
       int i = e >> 5, j = e & 31;
-      tri[i][j] = (i < np && j <= i) ? L[(long long)(p0 + i) * (p0 + i + 1) / 2 + p0 + j] : T(0);
+      tri[i][j] = (i < np && j <= i) ? L[rowoff<T>(p0 + i) + p0 + j] : T(0);
     }
     __syncthreads();
     if (w == 0) {
@@ -639,14 +654,31 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
 #pragma unroll
         for (int v = 0; v < NV; v++) acc[v] = T(0);
         if (i < nb) {
-          const T* Li = L + i * (i + 1) / 2 + p0 + sub * 8;
+          // rows below a panel only exist when the panel is full (np = 32): all 8 entries
+          // of the segment lie inside row i, 16-byte aligned
+          T lv[8];
+          const T* Li = L + rowoff<T>(i) + p0 + sub * 8;
+          if constexpr (sizeof(T) == 8) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const double2 t2 = reinterpret_cast<const double2*>(Li)[q];
+              lv[2 * q] = t2.x;
+              lv[2 * q + 1] = t2.y;
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+              const float4 t4 = reinterpret_cast<const float4*>(Li)[q];
+              lv[4 * q] = t4.x;
+              lv[4 * q + 1] = t4.y;
+              lv[4 * q + 2] = t4.z;
+              lv[4 * q + 3] = t4.w;
+            }
+          }
 #pragma unroll
           for (int q = 0; q < 8; q++)
-            if (sub * 8 + q < np) {
-              const T lv = Li[q];
 #pragma unroll
-              for (int v = 0; v < NV; v++) acc[v] = fma(lv, ysv[v][q], acc[v]);
-            }
+            for (int v = 0; v < NV; v++) acc[v] = fma(lv[q], ysv[v][q], acc[v]);
         }
 #pragma unroll
         for (int v = 0; v < NV; v++) {
@@ -668,7 +700,7 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
     for (int e = tid; e < 32 * 32; e += blockDim.x) {
       int i = e >> 5, j = e & 31;
       long long row = b0 + p0 + i;
-      tri[i][j] = (i < np && j <= i) ? L[row * (row + 1) / 2 + b0 + p0 + j] : T(0);
+      tri[i][j] = (i < np && j <= i) ? L[rowoff<T>(row) + b0 + p0 + j] : T(0);
     }
     __syncthreads();
     if (w == 0) {  // x_i = (y_i - sum_{j > i} L22[j][i] x_j) / L22[i][i], i = np-1 .. 0
@@ -696,7 +728,7 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
       for (int v = 0; v < NV; v++) acc[v] = T(0);
       for (int j = 0; j < np; j++) {
         long long row = b0 + p0 + j;
-        const T lv = L[row * (row + 1) / 2 + b0 + k];
+        const T lv = L[rowoff<T>(row) + b0 + k];
 #pragma unroll
         for (int v = 0; v < NV; v++) acc[v] = fma(lv, y[v * nb + b0 + p0 + j], acc[v]);
       }
@@ -862,7 +894,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   if (R.factor) {
     std::vector<long long> hl(ncell + 1);
     hl[0] = 0;
-    for (int c = 0; c < ncell; c++) hl[c + 1] = hl[c] + (long long)hcnt[c] * (hcnt[c] + 1) / 2;
+    for (int c = 0; c < ncell; c++) hl[c + 1] = hl[c] + (fp32 ? rowoff<float>(hcnt[c]) : rowoff<double>(hcnt[c]));
     R.loff.reserve(ncell + 1);
     PRBF_CUDA(cudaMemcpyAsync(R.loff.get(), hl.data(), sizeof(long long) * (ncell + 1), cudaMemcpyHostToDevice, s));
     if (fp32)
