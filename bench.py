@@ -471,6 +471,14 @@ def run_case(name):
         r = np.random.default_rng(1).standard_normal(len(x))
         for _ in range(3):
             c.pc_apply(r)
+    elif name == "chol32_2d":  # FP32 restricted blocks (S_c form), 400^2 jittered lattice, config-2 blocks
+        x, y, h = W.lattice_2d(400, jitter=0.25, seed=1)
+        c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
+        c.matvec_setup(x, y)
+        c.pc_setup("mixed")
+        r = np.random.default_rng(1).standard_normal(len(x))
+        for _ in range(3):
+            c.pc_apply(r)
     elif name == "batch":  # 24 problems of the batched form (N up to 6x10^4)
         batch_interpolate(W.config4(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
     else:
