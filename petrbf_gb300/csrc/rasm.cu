@@ -32,6 +32,7 @@ namespace {
 
 constexpr int TB = 64;         // tile edge
 constexpr int NTH = 256;       // threads per CTA (16 x 16, 4 x 4 outputs each)
+static_assert(NTH == 256 && TB == 64, "the tile kernels map 16 x 16 threads onto 4 x 4 outputs each");
 // inner chunk of the tile GEMM: FP32 is latency-bound on its operand loads, so it takes
 // wider chunks; FP64 is bound by the FP64 pipe and keeps shared memory small
 template <class T>
@@ -295,6 +296,8 @@ __device__ bool potrf_trtri(T* C, T* M, int h) {
     if (c > r) C[r * S + c] = T(0);
   }
   __syncthreads();
+  // each thread owns a fixed 4 x 4 sub-block (rows 4 ty .., columns 4 tx ..) of the tile
+  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
   for (int j = 0; j < h; j++) {
     T d = C[j * S + j];
     if (!(d > T(0))) {
@@ -307,11 +310,20 @@ __device__ bool potrf_trtri(T* C, T* M, int h) {
     for (int i = j + 1 + threadIdx.x; i < h; i += NTH) C[i * S + j] /= s;
     __syncthreads();
     if (threadIdx.x == 0) C[j * S + j] = s;
-    int rem = h - j - 1;
-    for (int e = threadIdx.x; e < rem * rem; e += NTH) {
-      int i = j + 1 + e / rem, l = j + 1 + e % rem;
-      if (l <= i) C[i * S + l] = fma(-C[i * S + j], C[l * S + j], C[i * S + l]);
+    T ci[4], cl[4];
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+      const int i = 4 * ty + p, l = 4 * tx + p;
+      ci[p] = (i > j && i < h) ? C[i * S + j] : T(0);
+      cl[p] = (l > j && l < h) ? C[l * S + j] : T(0);
     }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int i = 4 * ty + p, l = 4 * tx + q;
+        if (l > j && l <= i && i < h) C[i * S + l] = fma(-ci[p], cl[q], C[i * S + l]);
+      }
     __syncthreads();
   }
   // M = C^-1 (lower triangular), column by column: thread c owns column c
@@ -381,6 +393,295 @@ __host__ __device__ __forceinline__ long long rowoff(long long i) {
   return A * (A * q * (q + 1) / 2 + rr * (q + 1));
 }
 
+// ---- FP32 block Cholesky on the tensor cores (tcgen05, 3xTF32) ------------------------
+// The trailing updates C_ik -= sum_p L_ip L_kp^T and the panel solves L_ik = C_ik L_kk^-T
+// of the left-looking tile Cholesky are GEMMs: each runs as tcgen05.mma kind::tf32 with
+// M = 128 rows (two 64-row tiles of the column), N = 64, accumulating in TMEM. FP32
+// accuracy comes from splitting every operand x = hi + lo (hi = x rounded to TF32, lo =
+// the rest, also TF32): A B ~ Ahi Bhi + Ahi Blo + Alo Bhi. Operands go through shared
+// memory in 32-column chunks in the canonical K-major layout without swizzle (core
+// matrices of 8 rows x 16 bytes; element (r, k) at (r/8)*SBO + (k/4)*128 + (r%8)*16 +
+// (k%4)*4 bytes, SBO = 8 core matrices = 1024 bytes, LBO = 128 bytes). One elected thread
+// issues the MMAs and commits them to an mbarrier; the diagonal tiles are factored and
+// inverted on the CUDA cores (potrf_trtri). Writes L (lower part) over the dense block and,
+// for the S_c form, the diagonal inverses; k_chol_sc then runs its epilogues only.
+constexpr int TC_KCH = 32;  // K columns per operand chunk
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  constexpr uint32_t lbo = 128, sbo = (TC_KCH / 4) * 128;
+  uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(lbo >> 4) << 16;
+  d |= (uint64_t)(sbo >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05; base offset 0, no swizzle
+  return d;
+}
+
+__device__ __forceinline__ void tc_split(float x, float& hi, float& lo) {
+  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);  // TF32, nearest
+  lo = x - hi;
+}
+
+struct TcStage {
+  float* ahi;  // [128][TC_KCH] canonical
+  float* alo;
+  float* bhi;  // [64][TC_KCH]
+  float* blo;
+};
+
+// D (TMEM, 128 x 64 FP32) += A B^T over one staged chunk (TC_KCH = 4 MMAs of K = 8, 3 terms)
+__device__ __forceinline__ void tc_issue(uint32_t tmem, const TcStage& st, bool first) {
+  constexpr uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                             ((uint32_t)(128 >> 4) << 24);  // D F32, A/B TF32, K-major, N 64, M 128
+  const float* as[3] = {st.ahi, st.ahi, st.alo};
+  const float* bs[3] = {st.bhi, st.blo, st.bhi};
+#pragma unroll
+  for (int ks = 0; ks < TC_KCH / 8; ks++)
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+      const uint64_t da = tc_desc(tc_smem(as[t]) + ks * 256), db = tc_desc(tc_smem(bs[t]) + ks * 256);
+      const uint32_t acc = (first && ks == 0 && t == 0) ? 0u : 1u;
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(
+              tmem),
+          "l"(da), "l"(db), "r"(idesc), "r"(acc));
+    }
+}
+
+// Commit the issued MMAs (elected thread) and wait (all threads, bounded); false on timeout.
+__device__ __forceinline__ bool tc_commit_wait(uint64_t* bar, unsigned& phase) {
+  if (threadIdx.x == 0)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(bar))
+                 : "memory");
+  const bool ok = mbar_wait(bar, phase);
+  phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return ok;
+}
+
+__device__ __forceinline__ void tc_sync() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 32 columns of the thread's TMEM row: warp w reads lanes 32 (w % 4) .., column half w / 4
+__device__ __forceinline__ void tc_load32(uint32_t tmem, float v[32]) {
+  const int w = threadIdx.x >> 5;
+  const uint32_t addr = tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(32 * (w >> 2));
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// One operand chunk in registers: A rows [ar0, ar0 + 128) (valid below ar_end and at or
+// above ar_skip), columns [c0, c0 + 32) (valid below c_end) of the dense block, and B rows
+// [br0, br0 + 64) (valid below br_end) from the dense block (Msm null) or from the diagonal
+// inverse M in shared memory. Each warp instruction covers one core matrix (8 rows x 4
+// columns: lane l -> row l/4, column l%4), so the global loads touch 8 row segments of 16
+// bytes and the shared-memory stores are 32 consecutive words; all loads are issued before
+// any is used.
+struct TcRegs {
+  float a[16], b[8];
+};
+
+__device__ __forceinline__ void tc_fetch(TcRegs& R, const float* A, int nb, int ar0, int ar_skip, int ar_end, int c0,
+                                         int c_end, int br0, int br_end, const float* Msm, int mcol0) {
+  constexpr int S = SP<float>::S;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {  // A: core matrices w*16 + i (row group cm/8, column group cm%8)
+    const int cm = w * 16 + i, r = (cm >> 3) * 8 + (lane >> 2), k = (cm & 7) * 4 + (lane & 3);
+    const int row = ar0 + r;
+    R.a[i] = (row < ar_end && row >= ar_skip && c0 + k < c_end) ? A[(long long)row * nb + c0 + k] : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; i++) {  // B: core matrices w*8 + i
+    const int cm = w * 8 + i, r = (cm >> 3) * 8 + (lane >> 2), k = (cm & 7) * 4 + (lane & 3);
+    const int row = br0 + r;
+    float x = 0.f;
+    if (row < br_end) {
+      if (Msm)
+        x = Msm[r * S + mcol0 + k];
+      else if (c0 + k < c_end)
+        x = A[(long long)row * nb + c0 + k];
+    }
+    R.b[i] = x;
+  }
+}
+
+// Core matrix cm of a chunk occupies words [32 cm, 32 cm + 32) in the canonical layout.
+__device__ __forceinline__ void tc_store(const TcStage& st, const TcRegs& R) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    float h, l;
+    tc_split(R.a[i], h, l);
+    st.ahi[(w * 16 + i) * 32 + lane] = h;
+    st.alo[(w * 16 + i) * 32 + lane] = l;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    float h, l;
+    tc_split(R.b[i], h, l);
+    st.bhi[(w * 8 + i) * 32 + lane] = h;
+    st.blo[(w * 8 + i) * 32 + lane] = l;
+  }
+}
+
+size_t chol_tc_smem() {
+  return sizeof(float) * (2 * 128 * TC_KCH + 2 * 64 * TC_KCH + 2 * TB * SP<float>::S) + 64;
+}
+
+__global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restrict__ blk_cell,
+                                                     const long long* __restrict__ boff, const int* __restrict__ cs,
+                                                     const long long* __restrict__ koff, float* __restrict__ K,
+                                                     const long long* __restrict__ xoff, float* __restrict__ Xw,
+                                                     unsigned char* __restrict__ bad,
+                                                     const unsigned char* __restrict__ only, int mode,
+                                                     unsigned* __restrict__ err) {
+  const int b = blockIdx.x;
+  if (b >= nblk || (only && !only[b])) return;
+  constexpr int S = SP<float>::S;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float* base = (float*)smem_raw;
+  TcStage st;
+  st.ahi = base;
+  st.alo = st.ahi + 128 * TC_KCH;
+  st.bhi = st.alo + 128 * TC_KCH;
+  st.blo = st.bhi + 64 * TC_KCH;
+  float* Ct = st.blo + 64 * TC_KCH;  // [TB][S] diagonal tile
+  float* Mt = Ct + TB * S;           // [TB][S] its inverse
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, w = tid >> 5;
+
+  const int c = blk_cell[b];
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  const int nc = cs[c + 1] - cs[c], n1 = mode == 1 ? nb : nb - nc;
+  const int kc1 = (n1 + TB - 1) / TB;
+  const int ntile = kc1 + (mode == 1 ? 0 : (nc + TB - 1) / TB);
+  const int nct = ntile - kc1;
+  float* A = K + koff[b];
+  float* Minv_all = Xw + xoff[b] + (long long)nb * nct * TB;
+
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    s_abort = 0;
+  }
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_base)),
+                 "r"(64));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_sync();
+  const uint32_t tmem = tmem_base;
+  unsigned phase = 0;
+  bool ok = true;
+  const int r_own = 32 * (w & 3) + (tid & 31), cbase = 32 * (w >> 2);  // TMEM row / column half
+
+  for (int k = 0; k < ntile && !s_abort; k++) {
+    int rk, hk;
+    tile_range(k, n1, nb, kc1, rk, hk);
+    for (int pr = rk; pr < nb && !s_abort; pr += 128) {
+      // ---- update: C = A[pr.., rk..] - sum over columns [0, rk) (rows pr .. pr + 127)
+      if (rk > 0) {
+        // next chunk's loads in flight while the tensor cores work on this one
+        TcRegs R;
+        tc_fetch(R, A, nb, pr, pr, nb, 0, rk, rk, rk + hk, nullptr, 0);
+        for (int c0 = 0; c0 < rk; c0 += TC_KCH) {
+          tc_store(st, R);
+          tc_sync();
+          if (tid == 0) tc_issue(tmem, st, c0 == 0);
+          if (c0 + TC_KCH < rk) tc_fetch(R, A, nb, pr, pr, nb, c0 + TC_KCH, rk, rk, rk + hk, nullptr, 0);
+          if (!tc_commit_wait(&bar, phase)) {
+            if (tid == 0) {
+              atomicOr(err, DEV_ERR_TIMEOUT);
+              s_abort = 1;
+            }
+          }
+          __syncthreads();
+          if (s_abort) break;
+        }
+        if (s_abort) break;
+        float v[32];
+        tc_load32(tmem, v);
+        const int row = pr + r_own;
+        if (row < nb)
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const int col = cbase + j;
+            // the diagonal tile keeps its lower part; rows below take the whole tile width
+            if (col < hk && (row >= rk + hk || col <= row - rk)) A[(long long)row * nb + rk + col] -= v[j];
+          }
+        __syncthreads();
+      }
+      // ---- the diagonal tile (first panel of the column): factor and invert it
+      if (pr == rk) {
+        for (int e = tid; e < TB * TB; e += NTH) {
+          const int r = e / TB, cc = e % TB;
+          Ct[r * S + cc] = (r < hk && cc <= r) ? A[(long long)(rk + r) * nb + rk + cc] : 0.f;
+        }
+        __syncthreads();
+        ok = potrf_trtri<float>(Ct, Mt, hk) && ok;
+        for (int e = tid; e < TB * TB; e += NTH) {
+          const int r = e / TB, cc = e % TB;
+          if (r < hk && cc <= r) A[(long long)(rk + r) * nb + rk + cc] = Ct[r * S + cc];
+          if (mode == 0) Minv_all[(long long)k * TB * TB + e] = Mt[r * S + cc];
+        }
+        __syncthreads();
+      }
+      // ---- panel solve of the rows below the diagonal tile: L = C M^T (M = L_kk^-1)
+      if (pr + 128 > rk + hk && rk + hk < nb) {
+        TcRegs R;
+        for (int c0 = 0; c0 < TB; c0 += TC_KCH) {
+          tc_fetch(R, A, nb, pr, rk + hk, nb, rk + c0, rk + hk, 0, hk, Mt, c0);
+          tc_store(st, R);
+          tc_sync();
+          if (tid == 0) tc_issue(tmem, st, c0 == 0);
+          if (!tc_commit_wait(&bar, phase)) {
+            if (tid == 0) {
+              atomicOr(err, DEV_ERR_TIMEOUT);
+              s_abort = 1;
+            }
+          }
+          __syncthreads();
+          if (s_abort) break;
+        }
+        if (s_abort) break;
+        float v[32];
+        tc_load32(tmem, v);
+        const int row = pr + r_own;
+        __syncthreads();  // every thread has read its C row before any writes it over
+        if (row < nb && row >= rk + hk)
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const int col = cbase + j;
+            if (col < hk) A[(long long)row * nb + rk + col] = v[j];
+          }
+        __syncthreads();
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
+  if (tid == 0) bad[b] = (ok && !s_abort) ? 0 : 1;
+}
+
 // One CTA per block: Cholesky, centre columns of the inverse, S_c.
 template <class T>
 __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
@@ -391,7 +692,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
                                                  double out_scale_all, const double* __restrict__ cell_sig,
                                                  unsigned char* __restrict__ bad,
                                                  const unsigned char* __restrict__ only, int mode,
-                                                 const long long* __restrict__ loff, T* __restrict__ Lpack) {
+                                                 const long long* __restrict__ loff, T* __restrict__ Lpack,
+                                                 int skip_chol) {
   int b = blockIdx.x;
   if (b >= nblk || (only && !only[b])) return;
   // per-block scale (batches of problems with their own sigma): mode 1 sqrt(1/(2 pi s^2)),
@@ -425,9 +727,10 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
   const long long ldx = (long long)nct * TB;
   Minv_all = X + (long long)nb * ldx;    // ntile diagonal inverses, TB x TB each
   bool ok = true;
+  if (skip_chol) ok = bad[b] == 0;  // factored by k_chol_tc
 
   // ---- Cholesky, left-looking over tile columns -------------------------------------
-  for (int k = 0; k < ntile; k++) {
+  for (int k = 0; k < (skip_chol ? 0 : ntile); k++) {
     int rk, hk;
     tile_range(k, n1, nb, kc1, rk, hk);
     for (int i = k; i < ntile; i++) {
@@ -840,7 +1143,6 @@ void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff
 
 void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, const std::vector<int>& hcs, bool fp32,
                  Workspace& ws, unsigned* err, cudaStream_t s, double ws_budget_bytes, bool factor, bool basic) {
-  (void)err;
   const int ncell = G.ncell;
   R.fp32 = fp32;
   R.ncell = ncell;
@@ -911,9 +1213,10 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
   const double out_scale = 2.0 * M_PI * G.sigma * G.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
   size_t smem = fp32 ? chol_smem<float>() : chol_smem<double>();
-  if (fp32)
+  if (fp32) {
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  else
+    PRBF_CUDA(cudaFuncSetAttribute(k_chol_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_tc_smem()));
+  } else
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   R.nfallback = 0;
   size_t pos = 0;
@@ -958,14 +1261,18 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
         k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
                                              inv2s2, G.cell_sigma, shift, (float*)Kw, only);
         PRBF_CHECK_LAUNCH();
+        // the Cholesky on the tensor cores, then the factor / S_c epilogues of k_chol_sc
+        k_chol_tc<<<nb_batch, NTH, chol_tc_smem(), s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
+                                                        (float*)Xw, dbad, only, R.factor ? 1 : 0, err);
+        PRBF_CHECK_LAUNCH();
         if (R.factor)
           k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
                                                        (float*)Xw, R.soff.get(), nullptr, std::sqrt(1.0 / out_scale),
-                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get());
+                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get(), 1);
         else
           k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
                                                        (float*)Xw, R.soff.get(), R.S32.get(), out_scale,
-                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr);
+                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr, 1);
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
                                               G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only);
@@ -973,7 +1280,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
         k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (double*)Kw, dx,
                                                       (double*)Xw, R.soff.get(), nullptr,
                                                       std::sqrt(1.0 / out_scale), G.cell_sigma, dbad, only, 1,
-                                                      R.loff.get(), R.L64.get());
+                                                      R.loff.get(), R.L64.get(), 0);
       }
       PRBF_CHECK_LAUNCH();
       hbad.resize(nb_batch);
