@@ -180,6 +180,8 @@ typedef struct {
   double t_tune_ms;         /* autotuning (0 when the schedule came from the cache) */
   double t_solve_ms;        /* lockstep GMRES */
   double t_total_ms;
+  double t_matvec_ms;       /* one FP64 Gaussian sum over the whole batch (CUDA events, with
+                               the chosen schedule): pairs_per_matvec / t_matvec_ms is its rate */
 } prbf_batch_stats;
 
 /* Solves every problem with GMRES + Schwarz blocks in one set of launches per iteration

@@ -49,7 +49,8 @@ class BatchStats(ctypes.Structure):
                 ("min_block", ctypes.c_int), ("max_block", ctypes.c_int), ("nblocks_fallback", ctypes.c_int),
                 ("tile", ctypes.c_int), ("grid", ctypes.c_int), ("max_true_rel_resid", ctypes.c_double),
                 ("t_sort_ms", ctypes.c_double), ("t_setup_ms", ctypes.c_double), ("t_tune_ms", ctypes.c_double),
-                ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double)]
+                ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double),
+                ("t_matvec_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

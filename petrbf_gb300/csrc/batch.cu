@@ -337,6 +337,24 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   long long pairs_check = 0;
   upload_items(B.plan, make_items(B, sch.tile, &pairs_check), c.stream);
   B.plan.grid = sch.grid;
+  // one timed Gaussian sum with the chosen schedule (its rate is reported)
+  double t_mv = 0;
+  {
+    cudaEvent_t e0, e1;
+    PRBF_CUDA(cudaEventCreate(&e0));
+    PRBF_CUDA(cudaEventCreate(&e1));
+    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), false, c.err.get(), c.stream);
+    PRBF_CUDA(cudaEventRecord(e0, c.stream));
+    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), false, c.err.get(), c.stream);
+    PRBF_CUDA(cudaEventRecord(e1, c.stream));
+    PRBF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    PRBF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    t_mv = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    PRBF_CUDA(cudaMemsetAsync(B.tmp.get(), 0, sizeof(double) * ldv, c.stream));
+  }
   std::vector<long long> offs(B.poff.begin(), B.poff.end() - 1);
   if (!B.kry.same_layout(offs, B.n, p.restart)) B.kry.init(offs, B.n, ldv, p.restart, c.stream);
   B.kry.graph_op = nullptr;
@@ -406,6 +424,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   st.t_tune_ms = t_tune;
   st.t_solve_ms = t_solve;
   st.t_total_ms = now_ms() - t_begin;
+  st.t_matvec_ms = t_mv;
   if (bs) *bs = st;
   if (worst == -3) throw Error(PRBF_ERR_NOT_CONVERGED, "a problem of the batch reached the iteration limit");
   if (worst == -5) throw Error(PRBF_ERR_BREAKDOWN, "GMRES breakdown in a problem of the batch");

@@ -177,6 +177,26 @@ def cylinder_problem(x, y, e, overlap=0.9, nsigma_box=5, buffer_factor=1.9):
                    exact=e, meta={"overlap": overlap})
 
 
+def config4_lattice(nprob=256, seed=2025, nmin=2000, nmax=200000, nsigma_box=4):
+    """The lattice counterpart of config4: the same N distribution, each problem an m x m
+    lattice (m = round(sqrt(N))) over [-1,1]^2 with +/-0.25h seeded jitter, h = 2/m, h/sigma
+    uniform in [0.6, 1.0], Lamb-Oseen right-hand side as in config4."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nprob):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        m = max(8, int(round(math.sqrt(n))))
+        x, y, h = lattice_2d(m, jitter=0.25, seed=int(rng.integers(1 << 30)))
+        ratio = rng.uniform(0.6, 1.0)
+        xc, yc = rng.uniform(-0.5, 0.5, 2)
+        rc = rng.uniform(0.1, 0.3)
+        f = lamb_oseen(x, y, nu=rc * rc / 4.0, xc=xc, yc=yc)
+        out.append({"x": x, "y": y, "f": f, "sigma": h / ratio, "nsigma_box": nsigma_box,
+                    "sigma_buffer": 3 * nsigma_box, "sigma_trunc": nsigma_box + 16,
+                    "meta": {"n": m * m, "h_over_sigma": ratio, "centre": (xc, yc), "core_radius": rc}})
+    return out
+
+
 def log10_rel_error(w, e):
     """log10(||w - e||_2 / ||e||_2), 2d/main.cxx:130-133."""
     w = np.asarray(w, np.float64)
