@@ -99,6 +99,8 @@ typedef struct {
   double guess_rel_resid;   /* ||f - A g0||_2 / ||f||_2 of the learned guess (mixed) or its
                                preconditioned residual relative to ||B f|| (plain); 1 = zero */
   double t_guess_ms;        /* learned-guess inference */
+  int fp64_fallback;        /* mixed form: 1 if the refinement stalled (a system too
+                               ill-conditioned for FP32) and the call was solved in FP64 */
 } prbf_stats;
 
 typedef struct prbf_ctx prbf_ctx;
@@ -154,8 +156,11 @@ int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
 /* ---- batches of independent problems (no reference counterpart: the reference solves
  * one problem per call; this is the replica form for many small problems on one GPU) ---- */
 
-/* One problem of a batch; dimension, tolerances, restart, iteration limit and the Schwarz
- * type come from the context's parameters (FP64, zero guess). */
+/* One problem of a batch; dimension, tolerances, restart, iteration limit, precision and
+ * the Schwarz type come from the context's parameters (zero guess). PRBF_PREC_FP64 solves
+ * every problem with FP64 GMRES; PRBF_PREC_MIXED runs FP64 iterative refinement per
+ * problem (true residual ||f - A g||_2 <= rtol ||f||_2) around GMRES with FP32 Gaussian
+ * sums and FP32 block factors. */
 typedef struct {
   int n;
   const double *x, *y, *z;  /* caller-order coordinates (z null in 2D) */
@@ -182,6 +187,11 @@ typedef struct {
   double t_total_ms;
   double t_matvec_ms;       /* one FP64 Gaussian sum over the whole batch (CUDA events, with
                                the chosen schedule): pairs_per_matvec / t_matvec_ms is its rate */
+  double t_matvec32_ms;     /* the same for the FP32 sum (mixed form; else 0) */
+  int outer_its;            /* mixed form: refinement steps of the slowest problem */
+  int nprob_fp64;           /* mixed form: problems too ill-conditioned for FP32 (a block
+                               whose FP32 Cholesky needed a shift, or a refinement step that
+                               did not halve the FP64 residual), solved as an FP64 batch */
 } prbf_batch_stats;
 
 /* Solves every problem with GMRES + Schwarz blocks in one set of launches per iteration

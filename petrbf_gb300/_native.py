@@ -30,7 +30,8 @@ class Stats(ctypes.Structure):
                 ("t_sort_ms", ctypes.c_double), ("t_setup_ms", ctypes.c_double),
                 ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double),
                 ("pairs_per_matvec", ctypes.c_longlong), ("guess_used", ctypes.c_int),
-                ("guess_rel_resid", ctypes.c_double), ("t_guess_ms", ctypes.c_double)]
+                ("guess_rel_resid", ctypes.c_double), ("t_guess_ms", ctypes.c_double),
+                ("fp64_fallback", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -50,7 +51,8 @@ class BatchStats(ctypes.Structure):
                 ("tile", ctypes.c_int), ("grid", ctypes.c_int), ("max_true_rel_resid", ctypes.c_double),
                 ("t_sort_ms", ctypes.c_double), ("t_setup_ms", ctypes.c_double), ("t_tune_ms", ctypes.c_double),
                 ("t_solve_ms", ctypes.c_double), ("t_total_ms", ctypes.c_double),
-                ("t_matvec_ms", ctypes.c_double)]
+                ("t_matvec_ms", ctypes.c_double), ("t_matvec32_ms", ctypes.c_double),
+                ("outer_its", ctypes.c_int), ("nprob_fp64", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -152,10 +152,12 @@ class Context:
         return w
 
 
-def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="asm", device=0):
+def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="asm", device=0,
+                      precision="fp64"):
     """Solves many independent problems together. problems: sequence of dicts with keys x,
-    y, (z), f, sigma, nsigma_box, sigma_buffer, sigma_trunc. Returns (list of weight
-    arrays, iterations per problem, reason per problem, BatchStats)."""
+    y, (z), f, sigma, nsigma_box, sigma_buffer, sigma_trunc. precision "mixed": FP32 sums
+    and block factors inside FP64 refinement per problem. Returns (list of weight arrays,
+    iterations per problem, reason per problem, BatchStats)."""
     keep, probs, outs = [], [], []
     for q in problems:
         arrs = [_f64(q[k]) for k in ("x", "y")] + [_f64(q.get("z")), _f64(q["f"])]
@@ -170,7 +172,8 @@ def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="
     its = np.zeros(len(probs), np.int32)
     reason = np.zeros(len(probs), np.int32)
     st = N.BatchStats()
-    with Context(dim=dim, rtol=rtol, restart=restart, max_it=max_it, pc=pc, device=device) as c:
+    with Context(dim=dim, rtol=rtol, restart=restart, max_it=max_it, pc=pc, device=device,
+                 precision=precision) as c:
         code = N.lib().prbf_batch_interpolate(c.h, len(probs), arr, its.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                               reason.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                               ctypes.byref(st))

@@ -12,6 +12,14 @@
 //     first, each block with its problem's sigma) and applied in one launch;
 //   * GMRES runs one Krylov segment per problem, in lockstep, each with its own basis,
 //     Hessenberg matrix and stopping test (the same iterates as a solve of its own).
+// Mixed form: the sums and block factors are FP32 and GMRES solves the correction
+// equation of an FP64 iterative refinement run per problem (the single-problem mixed
+// form of solve.cu over all problems at once); a problem whose FP64 residual has met the
+// tolerance drops out of the FP64 residual sums as well. Refinement contracts by about
+// cond(A) u_fp32 per step, so a problem too ill-conditioned for FP32 -- one with a block
+// whose FP32 Cholesky met a non-positive pivot (cond(A) >= cond(block) ~ 1/u_fp32), or
+// whose refinement step did not halve its FP64 residual -- is solved again, with the
+// others of its kind, as an FP64 batch.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -58,8 +66,9 @@ struct BatchOp : Operator {
   PointsView v{};
   const RasmPlan* rasm = nullptr;
   unsigned* err = nullptr;
+  bool fp32 = false;
   void apply_A(const double* x, double* y, const int* skip, cudaStream_t s) const override {
-    gauss_sum_dev(*plan, v, v, x, y, false, err, s, skip);
+    gauss_sum_dev(*plan, v, v, x, y, fp32, err, s, skip);
   }
   void apply_B(const double* r, double* z, const int* skip, cudaStream_t s) const override {
     rasm_apply(*rasm, v.cell_start, r, z, s, skip);
@@ -87,13 +96,14 @@ struct BatchState {
   GaussPlan plan;
   RasmPlan rasm;
   Krylov kry;
-  BatchOp op;
-  DevBuf<double> b, sol, r, tmp;
+  BatchOp op, op32;
+  DevBuf<double> b, sol, r, tmp, d;
+  DevBuf<int> odone;  // mixed form: per problem, its FP64 residual met the tolerance
 };
 
 namespace {
-// Schedules picked by the autotuner, per device and batch shape (dimension, problems,
-// points), kept for the life of the process.
+// Schedules picked by the autotuner, per device and batch shape (precision, dimension,
+// problems, points), kept for the life of the process.
 std::map<std::pair<int, long long>, Schedule>& schedule_cache() {
   static std::map<std::pair<int, long long>, Schedule> m;
   return m;
@@ -135,9 +145,10 @@ void upload_items(GaussPlan& P, const std::vector<int2>& items, cudaStream_t s) 
   PRBF_CUDA(cudaStreamSynchronize(s));
 }
 
-// Times the batched FP64 sum for (tile, grid) candidates on a strided sample of the items
-// (an eighth, keeping the cost distribution) and keeps the fastest.
-Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout) {
+// Times the batched sum (FP64, or FP32 for the mixed form, whose iterations are FP32) for
+// (tile, grid) candidates on a strided sample of the items (an eighth, keeping the cost
+// distribution) and keeps the fastest.
+Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout, bool fp32) {
   const int tiles[3] = {32, 64, 128};
   const int grids[3] = {0, 152 * 3, 152 * 6};
   Schedule best;
@@ -151,9 +162,9 @@ Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout) {
     upload_items(B.plan, sample, c.stream);
     for (int grid : grids) {
       B.plan.grid = grid;
-      gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, false, c.err.get(), c.stream);  // warm-up
+      gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, fp32, c.err.get(), c.stream);  // warm-up
       PRBF_CUDA(cudaEventRecord(e0, c.stream));
-      for (int k = 0; k < 2; k++) gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, false, c.err.get(), c.stream);
+      for (int k = 0; k < 2; k++) gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, fp32, c.err.get(), c.stream);
       PRBF_CUDA(cudaEventRecord(e1, c.stream));
       PRBF_CUDA(cudaEventSynchronize(e1));
       float ms = 0;
@@ -177,7 +188,8 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   const prbf_params& p = c.p;
   const int dim = p.dim;
   if (nprob <= 0 || !probs) throw Error(PRBF_ERR_ARG, "empty batch");
-  if (p.precision != PRBF_PREC_FP64) throw Error(PRBF_ERR_ARG, "batches solve in FP64");
+  if (p.precision != PRBF_PREC_FP64 && p.precision != PRBF_PREC_MIXED) throw Error(PRBF_ERR_ARG, "bad precision");
+  const bool mixed = p.precision == PRBF_PREC_MIXED;
   if (p.guess != PRBF_GUESS_ZERO) throw Error(PRBF_ERR_ARG, "batches start from a zero guess");
   for (int i = 0; i < nprob; i++) {
     const prbf_problem& q = probs[i];
@@ -269,6 +281,10 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   B.plan.cprob.reserve(NC);
   PRBF_CUDA(cudaMemcpyAsync(B.plan.grids.get(), hgrids.data(), sizeof(Grid) * nprob, cudaMemcpyHostToDevice, c.stream));
   PRBF_CUDA(cudaMemcpyAsync(B.plan.cprob.get(), B.cprob.get(), sizeof(int) * NC, cudaMemcpyDeviceToDevice, c.stream));
+  B.plan.f32_ready = false;
+  if (mixed)
+    gauss_plan_f32_batch(B.plan, hgrids,
+                         PointsView{N, B.x.get(), B.y.get(), dim == 3 ? B.z.get() : nullptr, B.cs.get()}, c.stream);
 
   // ---- pass 2: buffer lists into the global block arrays, then one batched factorisation
   std::vector<long long> hb((size_t)NC + 1);
@@ -301,7 +317,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   G.cell_sigma = B.csig.get();
   size_t free_b = 0, total_b = 0;
   PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  rasm_factor(B.rasm, G, hcnt_all, B.hcs, false, c.ws, c.err.get(), c.stream, std::min(16.0e9, 0.25 * (double)free_b),
+  rasm_factor(B.rasm, G, hcnt_all, B.hcs, mixed, c.ws, c.err.get(), c.stream, std::min(16.0e9, 0.25 * (double)free_b),
               true, p.pc_type == PRBF_PC_ASM);
   rasm_set_apply_smem(B.rasm);
   c.check_device_error("batch RASM set-up");
@@ -312,8 +328,11 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   B.op.v = PointsView{N, B.x.get(), B.y.get(), dim == 3 ? B.z.get() : nullptr, B.cs.get()};
   B.op.rasm = &B.rasm;
   B.op.err = c.err.get();
+  B.op.fp32 = false;
+  B.op32 = B.op;
+  B.op32.fp32 = true;
   const long long ldv = (long long)N + 64;
-  for (auto* v : {&B.b, &B.sol, &B.r, &B.tmp}) {
+  for (auto* v : {&B.b, &B.sol, &B.r, &B.tmp, &B.d}) {
     v->reserve(ldv);
     PRBF_CUDA(cudaMemsetAsync(v->get(), 0, sizeof(double) * ldv, c.stream));
   }
@@ -322,7 +341,8 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
     gather_dev(B.n[i], B.perm.get() + B.poff[i], B.tmp.get(), B.b.get() + B.poff[i], c.stream);
   }
   PRBF_CUDA(cudaMemsetAsync(B.tmp.get(), 0, sizeof(double) * ldv, c.stream));
-  const std::pair<int, long long> key(c.device, ((long long)dim << 60) ^ ((long long)nprob << 40) ^ (long long)N);
+  const std::pair<int, long long> key(c.device, ((long long)(mixed ? 1 : 0) << 62) ^ ((long long)dim << 60) ^
+                                                    ((long long)nprob << 40) ^ (long long)N);
   Schedule sch;
   double t_tune = 0;
   auto hit = schedule_cache().find(key);
@@ -330,31 +350,31 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
     sch = hit->second;
   } else {
     const double tt0 = now_ms();
-    sch = autotune(c, B, B.b.get(), B.tmp.get());
+    sch = autotune(c, B, B.b.get(), B.tmp.get(), mixed);
     t_tune = now_ms() - tt0;
     schedule_cache()[key] = sch;
   }
   long long pairs_check = 0;
   upload_items(B.plan, make_items(B, sch.tile, &pairs_check), c.stream);
   B.plan.grid = sch.grid;
-  // one timed Gaussian sum with the chosen schedule (its rate is reported)
-  double t_mv = 0;
-  {
+  // one timed Gaussian sum with the chosen schedule, per precision in use (rates reported)
+  auto time_sum = [&](bool fp32) {
     cudaEvent_t e0, e1;
     PRBF_CUDA(cudaEventCreate(&e0));
     PRBF_CUDA(cudaEventCreate(&e1));
-    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), false, c.err.get(), c.stream);
+    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), fp32, c.err.get(), c.stream);
     PRBF_CUDA(cudaEventRecord(e0, c.stream));
-    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), false, c.err.get(), c.stream);
+    gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), fp32, c.err.get(), c.stream);
     PRBF_CUDA(cudaEventRecord(e1, c.stream));
     PRBF_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
     PRBF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    t_mv = ms;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     PRBF_CUDA(cudaMemsetAsync(B.tmp.get(), 0, sizeof(double) * ldv, c.stream));
-  }
+    return (double)ms;
+  };
+  const double t_mv = time_sum(false), t_mv32 = mixed ? time_sum(true) : 0.0;
   std::vector<long long> offs(B.poff.begin(), B.poff.end() - 1);
   if (!B.kry.same_layout(offs, B.n, p.restart)) B.kry.init(offs, B.n, ldv, p.restart, c.stream);
   B.kry.graph_op = nullptr;
@@ -371,8 +391,108 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   B.rasm.seg = seg;
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double ts0 = now_ms();
-  std::vector<KResult> kr =
-      B.kry.solve(B.op, B.b.get(), B.sol.get(), true, p.rtol, p.abstol, p.dtol, p.max_it, true, c.stream);
+  std::vector<int> its(nprob, 0), reason(nprob, 0), outer(nprob, 0);
+  std::vector<char> to64(nprob, 0);  // mixed form: problems handed to the FP64 batch
+  std::vector<double> true_rel(nprob, 0.0);
+  bool resid_current = false;
+  if (!mixed) {
+    std::vector<KResult> kr =
+        B.kry.solve(B.op, B.b.get(), B.sol.get(), true, p.rtol, p.abstol, p.dtol, p.max_it, true, c.stream);
+    for (int i = 0; i < nprob; i++) {
+      its[i] = kr[i].its;
+      reason[i] = kr[i].reason;
+    }
+  } else {
+    // FP64 iterative refinement of every problem: r = f - A g (FP64 sums, skipping the
+    // problems that have stopped), stop test on ||r|| <= rtol ||f||, then A d = r by GMRES
+    // with FP32 operators to 1e-6 and g += d in FP64.
+    B.odone.reserve(nprob);
+    PRBF_CUDA(cudaMemsetAsync(B.odone.get(), 0, sizeof(int) * nprob, c.stream));
+    SegSkip oseg;
+    oseg.cprob = B.cprob.get();
+    oseg.done = B.odone.get();
+    oseg.stride = 1;
+    std::vector<double> bnorm = seg_norm2_host(B.kry, B.b.get(), c.stream);
+    for (auto& q : bnorm) q = std::sqrt(q);
+    std::vector<double> rnorm(nprob, 0.0), prev(nprob, 0.0);
+    std::vector<int> hdone(nprob, 0);
+    // problems with a block that needed a shifted FP32 factorisation go to FP64 at once
+    for (int cell : B.rasm.retried) {
+      int i = (int)(std::upper_bound(B.coff.begin(), B.coff.end(), cell) - B.coff.begin()) - 1;
+      if (i >= 0 && i < nprob) to64[i] = 1;
+    }
+    bool xzero = true;
+    int inner_max = 0;
+    for (int it = 0; it < 50; it++) {
+      if (xzero) {
+        PRBF_CUDA(cudaMemcpyAsync(B.r.get(), B.b.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, c.stream));
+      } else {
+        B.plan.seg = oseg;
+        B.op.apply_A(B.sol.get(), B.tmp.get(), nullptr, c.stream);
+        B.plan.seg = seg;  // the correction solve skips on the Krylov stop flags
+        PRBF_CUDA(cudaMemcpyAsync(B.r.get(), B.b.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, c.stream));
+        axpy_dev(N, -1.0, B.tmp.get(), B.r.get(), c.stream);
+      }
+      std::vector<double> rn = seg_norm2_host(B.kry, B.r.get(), c.stream);
+      bool all = true, newly = false;
+      for (int i = 0; i < nprob; i++) {
+        if (!reason[i] && !to64[i]) {
+          const double q = std::sqrt(rn[i]);
+          rnorm[i] = q;
+          if (!(q == q) || std::isinf(q)) {
+            to64[i] = 1;
+          } else if (q <= p.rtol * bnorm[i] || q <= p.abstol) {
+            reason[i] = q <= p.abstol ? 3 : 2;
+          } else if (it > 0 && !(q <= 0.5 * prev[i])) {
+            to64[i] = 1;
+          } else if (inner_max >= p.max_it) {
+            reason[i] = -3;
+          } else {
+            outer[i]++;
+            prev[i] = q;
+            all = false;
+            continue;
+          }
+        }
+        // stopped: out of the correction solve (a zero residual stops at once) and out of
+        // the next FP64 residual sums
+        PRBF_CUDA(cudaMemsetAsync(B.r.get() + B.poff[i], 0, sizeof(double) * B.n[i], c.stream));
+        if (!hdone[i]) {
+          hdone[i] = 1;
+          newly = true;
+        }
+      }
+      if (newly)
+        PRBF_CUDA(cudaMemcpyAsync(B.odone.get(), hdone.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice, c.stream));
+      if (all) {
+        resid_current = true;
+        for (int i = 0; i < nprob; i++) true_rel[i] = bnorm[i] > 0 ? rnorm[i] / bnorm[i] : rnorm[i];
+        break;
+      }
+      PRBF_CUDA(cudaMemsetAsync(B.d.get(), 0, sizeof(double) * ldv, c.stream));
+      const int budget_its = std::min(p.max_it - inner_max, 4 * p.restart);
+      std::vector<KResult> in =
+          B.kry.solve(B.op32, B.r.get(), B.d.get(), true, 1e-6, 0.0, 1e10, budget_its, true, c.stream);
+      int step = 0;
+      bool progress = false;
+      for (int i = 0; i < nprob; i++) {
+        if (reason[i] || to64[i]) continue;
+        its[i] += in[i].its;
+        step = std::max(step, in[i].its);
+        progress = progress || in[i].its > 0;
+      }
+      inner_max += step;
+      axpy_dev(N, 1.0, B.d.get(), B.sol.get(), c.stream);
+      xzero = false;
+      if (!progress) {
+        for (int i = 0; i < nprob; i++)
+          if (!reason[i]) to64[i] = 1;
+        break;
+      }
+    }
+    for (int i = 0; i < nprob; i++)
+      if (!reason[i] && !to64[i]) reason[i] = -3;
+  }
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double t_solve = now_ms() - ts0;
   B.plan.seg = SegSkip{};
@@ -386,10 +506,17 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
     PRBF_CUDA(cudaMemcpyAsync(probs[i].g_out, B.tmp.get(), sizeof(double) * B.n[i], cudaMemcpyDeviceToHost, c.stream));
     PRBF_CUDA(cudaStreamSynchronize(c.stream));
   }
-  B.op.apply_A(B.sol.get(), B.r.get(), nullptr, c.stream);
-  PRBF_CUDA(cudaMemcpyAsync(B.tmp.get(), B.b.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, c.stream));
-  axpy_dev(N, -1.0, B.r.get(), B.tmp.get(), c.stream);
-  std::vector<double> rr = seg_norm2_host(B.kry, B.tmp.get(), c.stream), bn = seg_norm2_host(B.kry, B.b.get(), c.stream);
+  if (!resid_current) {
+    B.op.apply_A(B.sol.get(), B.r.get(), nullptr, c.stream);
+    PRBF_CUDA(cudaMemcpyAsync(B.tmp.get(), B.b.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, c.stream));
+    axpy_dev(N, -1.0, B.r.get(), B.tmp.get(), c.stream);
+    std::vector<double> rr = seg_norm2_host(B.kry, B.tmp.get(), c.stream),
+                        bn = seg_norm2_host(B.kry, B.b.get(), c.stream);
+    for (int i = 0; i < nprob; i++) {
+      double q = std::sqrt(rr[i]), bq = std::sqrt(bn[i]);
+      true_rel[i] = bq > 0 ? q / bq : q;
+    }
+  }
   prbf_batch_stats st{};
   st.nprob = nprob;
   st.points = N;
@@ -407,24 +534,51 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   st.nblocks_fallback = B.rasm.nfallback;
   st.tile = sch.tile;
   st.grid = sch.grid;
+  // problems too ill-conditioned for FP32: one FP64 batch of their own (it reuses this
+  // context's batch state, whose results have all been read back above)
+  std::vector<int> sub_idx;
+  for (int i = 0; i < nprob; i++)
+    if (to64[i]) sub_idx.push_back(i);
+  prbf_batch_stats sst{};
+  if (!sub_idx.empty()) {
+    std::vector<prbf_problem> sub;
+    for (int i : sub_idx) sub.push_back(probs[i]);
+    std::vector<int> sits(sub.size()), sreason(sub.size());
+    struct Restore {
+      prbf_params& p;
+      int prec;
+      ~Restore() { p.precision = prec; }
+    } restore{c.p, c.p.precision};
+    c.p.precision = PRBF_PREC_FP64;
+    batch_interpolate(c, (int)sub.size(), sub.data(), sits.data(), sreason.data(), &sst);
+    for (size_t k = 0; k < sub_idx.size(); k++) {
+      its[sub_idx[k]] += sits[k];
+      reason[sub_idx[k]] = sreason[k];
+      true_rel[sub_idx[k]] = 0.0;
+    }
+    st.max_true_rel_resid = std::max(st.max_true_rel_resid, sst.max_true_rel_resid);
+    st.nprob_fp64 = (int)sub_idx.size();
+    st.nblocks_fallback += sst.nblocks_fallback;
+  }
   int worst = 0;
   for (int i = 0; i < nprob; i++) {
-    double q = std::sqrt(rr[i]), bq = std::sqrt(bn[i]);
-    double rel = bq > 0 ? q / bq : q;
-    st.max_true_rel_resid = std::max(st.max_true_rel_resid, rel);
-    st.max_its = std::max(st.max_its, kr[i].its);
-    st.total_its += kr[i].its;
-    st.nconverged += kr[i].reason > 0 ? 1 : 0;
-    if (kr[i].reason < 0 && worst == 0) worst = kr[i].reason;
-    if (its_out) its_out[i] = kr[i].its;
-    if (reason_out) reason_out[i] = kr[i].reason;
+    st.max_true_rel_resid = std::max(st.max_true_rel_resid, true_rel[i]);
+    st.max_its = std::max(st.max_its, its[i]);
+    st.outer_its = std::max(st.outer_its, outer[i]);
+    st.total_its += its[i];
+    st.nconverged += reason[i] > 0 ? 1 : 0;
+    if (reason[i] < 0 && worst == 0) worst = reason[i];
+    if (its_out) its_out[i] = its[i];
+    if (reason_out) reason_out[i] = reason[i];
   }
-  st.t_sort_ms = t_sorted - t_begin;
-  st.t_setup_ms = t_setup - t_sorted;
-  st.t_tune_ms = t_tune;
-  st.t_solve_ms = t_solve;
+  // (the FP64 batch of the mixed form's ill-conditioned problems counts in each phase)
+  st.t_sort_ms = t_sorted - t_begin + sst.t_sort_ms;
+  st.t_setup_ms = t_setup - t_sorted + sst.t_setup_ms;
+  st.t_tune_ms = t_tune + sst.t_tune_ms;
+  st.t_solve_ms = t_solve + sst.t_solve_ms;
   st.t_total_ms = now_ms() - t_begin;
   st.t_matvec_ms = t_mv;
+  st.t_matvec32_ms = t_mv32;
   if (bs) *bs = st;
   if (worst == -3) throw Error(PRBF_ERR_NOT_CONVERGED, "a problem of the batch reached the iteration limit");
   if (worst == -5) throw Error(PRBF_ERR_BREAKDOWN, "GMRES breakdown in a problem of the batch");

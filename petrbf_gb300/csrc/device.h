@@ -105,6 +105,9 @@ struct GaussPlan {
 // Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc.
 void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src,
                     unsigned* err, Workspace& ws, cudaStream_t s);
+// FP32 form's source data of a batch (each problem with its own grid and scale, grids with
+// their first global cell); sets plan.f32_ready when every grid qualifies.
+void gauss_plan_f32_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src, cudaStream_t s);
 // w[i] = sum_{j in trunc(cell(i))} g[j] exp(-|t_i - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
 // for all sorted targets i; g must be a padded device vector of src.n (+2) entries.
 // w = A g for nv weight vectors at stride vstride (even; vectors padded as the sources)

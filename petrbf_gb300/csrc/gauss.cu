@@ -468,13 +468,16 @@ struct LayoutF {
   static constexpr size_t total = bar + 16;
 };
 
-template <int DIM, int NV>
+// BATCH: as k_gauss (the item's cell indexes a concatenation of grids); the source data
+// of each problem were built with its own grid and scale.
+template <int DIM, int NV, bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
-    Grid g, const int2* __restrict__ items, int nitems, const double* __restrict__ tx, const double* __restrict__ ty,
+    Grid g0, const Grid* __restrict__ grids, const int* __restrict__ cprob, SegSkip seg,
+    const int2* __restrict__ items, int nitems, const double* __restrict__ tx, const double* __restrict__ ty,
     const double* __restrict__ tz, const int* __restrict__ cs_t, const float* __restrict__ su,
     const float* __restrict__ sv, const float* __restrict__ sw, const unsigned long long* __restrict__ smask,
     const float* __restrict__ sg, long long vs_g, const int* __restrict__ cs_s, double* __restrict__ w,
-    long long vs_w, double scale, double norm, unsigned* err, const int* __restrict__ skip) {
+    long long vs_w, double scale0, double norm0, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
   using Lay = LayoutF<DIM, NV>;
   constexpr int NF = Lay::NF, KC = Lay::kComp, RC = Lay::RC;
@@ -497,17 +500,27 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
   if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
   const int G = gridDim.x;
-  const float boxs = (float)(g.box * scale);
-  const int nb = g.nb_trunc;
 
   for (int round = 0; (long long)round * G < nitems; round++) {
     const int it = (round & 1) ? round * G + (G - 1 - (int)blockIdx.x) : round * G + (int)blockIdx.x;
     if (it >= nitems) continue;
     const int2 item = items[it];
     const int ic = item.x, t0 = item.y;
+    Grid g = g0;
+    double scale = scale0, norm = norm0;
+    if constexpr (BATCH) {
+      if (seg.cell_done(ic)) continue;  // a stopped problem (uniform over the CTA)
+      g = grids[cprob[ic]];
+      const SumConsts k = sum_consts(g.sigma, true, 0);
+      scale = k.scale;
+      norm = k.norm;
+    }
+    const int cb = g.cbase;
+    const float boxs = (float)(g.box * scale);
+    const int nb = g.nb_trunc;
     const int nt = min(kTileT, cs_t[ic + 1] - t0);
     int ix, iy, iz;
-    cell_xyz(g, ic, ix, iy, iz);
+    cell_xyz(g, ic - cb, ix, iy, iz);
     const double xc = centre_coord(g.xmin, ix, g.box);
     const double yc = centre_coord(g.ymin, iy, g.box);
     const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
@@ -521,8 +534,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
     __syncthreads();
     for (int r = tid; r < min(nranges, kMaxRanges); r += kThreads) {
       const int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
-      s_ra[r] = cs_s[cell_of(g, jx, jy0, jz)];
-      s_rb[r] = cs_s[cell_of(g, jx, jy1, jz) + 1];
+      s_ra[r] = cs_s[cb + cell_of(g, jx, jy0, jz)];
+      s_rb[r] = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
     }
     for (int t = tid; t < nt; t += kThreads) {
       tgt[t] = (float)((tx[t0 + t] - xc) * scale);
@@ -595,8 +608,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
             a = s_ra[r];
             b = s_rb[r];
           } else {
-            a = cs_s[cell_of(g, jx, jy0, jz)];
-            b = cs_s[cell_of(g, jx, jy1, jz) + 1];
+            a = cs_s[cb + cell_of(g, jx, jy0, jz)];
+            b = cs_s[cb + cell_of(g, jx, jy1, jz) + 1];
           }
           int s = p < 0 ? a : p;
           if (s >= b) {
@@ -851,7 +864,7 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   PRBF_CHECK_LAUNCH();
 }
 
-template <int DIM, int NV>
+template <int DIM, int NV, bool BATCH>
 void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
                  long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
   constexpr size_t sm = LayoutF<DIM, NV>::total;
@@ -860,32 +873,38 @@ void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, c
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
-    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_f32m<DIM, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_f32m<DIM, NV, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
   const SumConsts k0 = sum_consts(P.g.sigma, true, 0);
   k_to_f32<<<4 * 152, 256, 0, st>>>(s.n, NV, vstride, P.g32_stride, gv, P.g32.get(), skip);
   PRBF_CHECK_LAUNCH();
   const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
-  k_gauss_f32m<DIM, NV><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, t.x, t.y, t.z, t.cell_start,
-                                                     P.su.get(), P.sv.get(), P.sw.get(), P.smask.get(), P.g32.get(),
-                                                     P.g32_stride, s.cell_start, w, vstride, k0.scale, k0.norm, err,
-                                                     skip);
+  k_gauss_f32m<DIM, NV, BATCH><<<grid, kThreads, sm, st>>>(
+      P.g, P.grids.get(), P.cprob.get(), P.seg, P.items.get(), P.nitems, t.x, t.y, t.z, t.cell_start, P.su.get(),
+      P.sv.get(), P.sw.get(), P.smask.get(), P.g32.get(), P.g32_stride, s.cell_start, w, vstride, k0.scale, k0.norm,
+      err, skip);
   PRBF_CHECK_LAUNCH();
 }
 
 template <int DIM, bool F32>
 void launch_nv(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w, int nv,
                long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
-  if (F32 && P.f32_ready && !P.batched) {
+  if (F32 && P.f32_ready && P.batched) {
+    for (int v = 0; v < nv; v++)
+      launch_f32m<DIM, 1, true>(P, t, s, gv + v * vstride, w + v * vstride, vstride, err, skip, st);
+    return;
+  }
+  if (F32 && P.f32_ready) {
     for (int v0 = 0; v0 < nv; v0 += 4) {
       const double* g0 = gv + v0 * vstride;
       double* w0 = w + v0 * vstride;
       switch (std::min(4, nv - v0)) {
-        case 1: launch_f32m<DIM, 1>(P, t, s, g0, w0, vstride, err, skip, st); break;
-        case 2: launch_f32m<DIM, 2>(P, t, s, g0, w0, vstride, err, skip, st); break;
-        case 3: launch_f32m<DIM, 3>(P, t, s, g0, w0, vstride, err, skip, st); break;
-        default: launch_f32m<DIM, 4>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        case 1: launch_f32m<DIM, 1, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        case 2: launch_f32m<DIM, 2, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        case 3: launch_f32m<DIM, 3, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
+        default: launch_f32m<DIM, 4, false>(P, t, s, g0, w0, vstride, err, skip, st); break;
       }
     }
     return;
@@ -907,6 +926,23 @@ void launch_nv(const GaussPlan& P, const PointsView& t, const PointsView& s, con
 }
 
 }  // namespace
+
+// The FP32 form's masks hold 2 nb_trunc + 1 bits per axis and the cell y in 16 bits.
+static bool f32_grid_ok(const Grid& g) { return 2 * g.nb_trunc + 1 <= kMaskBits && g.ny < 65536; }
+
+static void alloc_f32(GaussPlan& plan, int dim, int n, cudaStream_t s) {
+  const long long n8 = (long long)n + 8;
+  plan.su.reserve(n8);
+  plan.sv.reserve(n8);
+  plan.sw.reserve(dim == 3 ? n8 : 1);
+  plan.smask.reserve(n8);
+  plan.g32_stride = ((long long)n + 8 + 31) / 32 * 32;
+  plan.g32.reserve(4 * plan.g32_stride);
+  PRBF_CUDA(cudaMemsetAsync(plan.g32.get(), 0, sizeof(float) * 4 * plan.g32_stride, s));
+  for (auto* b : {&plan.su, &plan.sv}) PRBF_CUDA(cudaMemsetAsync(b->get(), 0, sizeof(float) * n8, s));
+  if (dim == 3) PRBF_CUDA(cudaMemsetAsync(plan.sw.get(), 0, sizeof(float) * n8, s));
+  PRBF_CUDA(cudaMemsetAsync(plan.smask.get(), 0, sizeof(unsigned long long) * n8, s));
+}
 
 void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src, unsigned* err,
                     Workspace& ws, cudaStream_t s) {
@@ -944,24 +980,31 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
   upload_table(s);
   // FP32 form's source data
   plan.f32_ready = false;
-  if (2 * g.nb_trunc + 1 <= kMaskBits && g.ny < 65536 && src.n > 0) {
-    const long long n8 = (long long)src.n + 8;
-    plan.su.reserve(n8);
-    plan.sv.reserve(n8);
-    plan.sw.reserve(g.dim == 3 ? n8 : 1);
-    plan.smask.reserve(n8);
-    plan.g32_stride = ((long long)src.n + 8 + 31) / 32 * 32;
-    plan.g32.reserve(4 * plan.g32_stride);
-    PRBF_CUDA(cudaMemsetAsync(plan.g32.get(), 0, sizeof(float) * 4 * plan.g32_stride, s));
-    for (auto* b : {&plan.su, &plan.sv}) PRBF_CUDA(cudaMemsetAsync(b->get(), 0, sizeof(float) * n8, s));
-    if (g.dim == 3) PRBF_CUDA(cudaMemsetAsync(plan.sw.get(), 0, sizeof(float) * n8, s));
-    PRBF_CUDA(cudaMemsetAsync(plan.smask.get(), 0, sizeof(unsigned long long) * n8, s));
+  if (f32_grid_ok(g) && src.n > 0) {
+    alloc_f32(plan, g.dim, src.n, s);
     const SumConsts k32 = sum_consts(g.sigma, true, 0);
     k_src_f32<<<ceil_div(g.ncell, 128), 128, 0, s>>>(g, src.cell_start, src.x, src.y, src.z, k32.scale,
                                                      plan.su.get(), plan.sv.get(), plan.sw.get(), plan.smask.get());
     PRBF_CHECK_LAUNCH();
     plan.f32_ready = true;
   }
+}
+
+void gauss_plan_f32_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src, cudaStream_t s) {
+  plan.f32_ready = false;
+  if (src.n <= 0) return;
+  for (const Grid& g : grids)
+    if (!f32_grid_ok(g)) return;
+  alloc_f32(plan, grids[0].dim, src.n, s);
+  for (const Grid& g : grids) {
+    // the problem's cells are cell_start[cbase .. cbase + ncell]; its points keep their
+    // global positions
+    const SumConsts k32 = sum_consts(g.sigma, true, 0);
+    k_src_f32<<<ceil_div(g.ncell, 128), 128, 0, s>>>(g, src.cell_start + g.cbase, src.x, src.y, src.z, k32.scale,
+                                                     plan.su.get(), plan.sv.get(), plan.sw.get(), plan.smask.get());
+    PRBF_CHECK_LAUNCH();
+  }
+  plan.f32_ready = true;
 }
 
 void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv,

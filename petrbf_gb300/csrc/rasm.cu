@@ -1219,6 +1219,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   } else
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   R.nfallback = 0;
+  R.retried.clear();
   size_t pos = 0;
   std::vector<long long> hk, hx;
   std::vector<int> bc;
@@ -1287,7 +1288,10 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       PRBF_CUDA(cudaMemcpyAsync(hbad.data(), dbad, nb_batch, cudaMemcpyDeviceToHost, s));
       PRBF_CUDA(cudaStreamSynchronize(s));
       int nbad = 0;
-      for (unsigned char v : hbad) nbad += v ? 1 : 0;
+      for (int k = 0; k < nb_batch; k++) {
+        nbad += hbad[k] ? 1 : 0;
+        if (hbad[k] && attempt == 0) R.retried.push_back(bc[k]);
+      }
       if (nbad == 0) break;
       if (attempt == 2) throw Error(PRBF_ERR_FACTOR, "subdomain block not positive definite after shifted retries");
       R.nfallback += nbad;

@@ -13,6 +13,7 @@ struct RasmPlan {
   int ncell = 0, nblocks = 0;
   int max_nb = 0, max_nc = 0;
   int nfallback = 0;          // blocks that needed a diagonal-shift retry
+  std::vector<int> retried;   // their cells (host)
   DevBuf<long long> boff;     // buffer-list offsets per cell (ncell + 1)
   DevBuf<int> idx;            // buffer lists (sorted positions), centre first
   DevBuf<long long> soff;     // S_c offsets per cell (n_c * n_b each)

@@ -8,7 +8,10 @@
 // Mixed form (PRBF_PREC_MIXED): FP64 iterative refinement, x += d with A d = r solved
 // approximately by GMRES whose matvec and RASM blocks are FP32; FP64 is kept for the outer
 // residual matvec, the Arnoldi vectors and Hessenberg least squares, and the update. It
-// stops on the true residual ||f - A g||_2 <= rtol ||f||_2.
+// stops on the true residual ||f - A g||_2 <= rtol ||f||_2. Refinement contracts the
+// residual by about cond(A) u_fp32 per step, so a system too ill-conditioned for FP32
+// (tightly clustered points) stalls: a step that does not halve the FP64 residual, or a
+// non-finite one, hands the call to the plain form (FP64 blocks, FP64 GMRES from zero).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -160,37 +163,43 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   // true residual of the final weights and the reported one needs no extra matvec
   std::vector<double> true_rel(nv, 0.0);
   bool resid_current = false;
-  if (!mixed) {
+  // the plain form: GMRES on A x = b with the FP64 operators (from the guess in x, or zero)
+  auto plain_solve = [&](bool from_guess) {
     std::vector<double> ref(nv, 0.0);
-    if (use_guess) {
+    if (from_guess) {
       // converge relative to the zero-guess residual ||B b||, whatever the guess
       S.op64.apply_B(S.b.get(), S.tmp.get(), nullptr, c.stream);
       std::vector<double> q = seg_norm2_host(S.kry, S.tmp.get(), c.stream);
       for (int v = 0; v < nv; v++) ref[v] = std::sqrt(q[v]);
     }
-    std::vector<KResult> kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), !use_guess, p.rtol, p.abstol, p.dtol, p.max_it,
-                                          true, c.stream, use_guess ? ref.data() : nullptr, use_guess);
+    std::vector<KResult> kr = S.kry.solve(S.op64, S.b.get(), S.x.get(), !from_guess, p.rtol, p.abstol, p.dtol,
+                                          p.max_it, true, c.stream, from_guess ? ref.data() : nullptr, from_guess);
     int used = 0;
     double gres = 0;
     for (int v = 0; v < nv; v++) {
-      its[v] = kr[v].its;
+      its[v] += kr[v].its;
       reason[v] = kr[v].reason;
       rnorm0[v] = kr[v].rnorm0;
       rnorm[v] = kr[v].rnorm;
       used += kr[v].guess_used ? 1 : 0;
       gres = std::max(gres, ref[v] > 0 ? kr[v].guess_beta / ref[v] : 1.0);
     }
-    if (use_guess) {
+    if (from_guess) {
       st.guess_used = used == nv ? 1 : 0;
       st.guess_rel_resid = gres;
     }
+  };
+  if (!mixed) {
+    plain_solve(use_guess);
   } else {
     std::vector<double> bnorm = seg_norm2_host(S.kry, S.b.get(), c.stream);
     for (auto& q : bnorm) q = std::sqrt(q);
     bool xzero = !use_guess;
     int inner_max = 0;
     const int nall = (int)(ldn * nv);
-    for (int it = 0; it < 50; it++) {
+    std::vector<double> prev(nv, 0.0);
+    bool stalled = false;
+    for (int it = 0; it < 50 && !stalled; it++) {
       // r = b - A x in FP64 (all right-hand sides)
       if (xzero) {
         PRBF_CUDA(cudaMemcpyAsync(S.r.get(), S.b.get(), sizeof(double) * nall, cudaMemcpyDeviceToDevice, c.stream));
@@ -228,19 +237,24 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
           continue;
         }
         rnorm[v] = rn[v];
-        if (!(rn[v] == rn[v])) {
-          reason[v] = -9;
+        if (!(rn[v] == rn[v]) || std::isinf(rn[v])) {
+          stalled = true;
         } else if (rn[v] <= p.rtol * bnorm[v] || rn[v] <= p.abstol) {
           reason[v] = rn[v] <= p.abstol ? 3 : 2;
+        } else if (it > 0 && !(rn[v] <= 0.5 * prev[v])) {
+          stalled = true;
         } else if (inner_max >= p.max_it) {
           reason[v] = -3;
         } else {
           outer[v]++;
+          prev[v] = rn[v];
           all = false;
           continue;
         }
+        if (stalled) break;
         PRBF_CUDA(cudaMemsetAsync(S.r.get() + v * ldn, 0, sizeof(double) * n, c.stream));
       }
+      if (stalled) break;
       if (all) {
         resid_current = true;
         for (int v = 0; v < nv; v++) true_rel[v] = bnorm[v] > 0 ? rnorm[v] / bnorm[v] : rnorm[v];
@@ -261,14 +275,24 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
       inner_max += step;
       axpy_dev(nall, 1.0, S.d.get(), S.x.get(), c.stream);
       xzero = false;
-      if (!progress) {
-        for (int v = 0; v < nv; v++)
-          if (!reason[v]) reason[v] = -5;
-        break;
-      }
+      if (!progress) stalled = true;
     }
-    for (int v = 0; v < nv; v++)
-      if (!reason[v]) reason[v] = -3;
+    if (stalled) {
+      // FP64 blocks and FP64 GMRES from zero for every right-hand side (the inner
+      // iterations spent so far stay counted)
+      S.kry.reset_graph();
+      rasm_build(S.rasm, S.pts, false, c.ws, c.err.get(), c.stream, budget, false, p.pc_type == PRBF_PC_ASM);
+      rasm_set_apply_smem(S.rasm);
+      c.check_device_error("RASM set-up (FP64 fallback)");
+      PRBF_CUDA(cudaMemsetAsync(S.x.get(), 0, sizeof(double) * len_all, c.stream));
+      std::fill(reason.begin(), reason.end(), 0);
+      st.fp64_fallback = 1;
+      resid_current = false;
+      plain_solve(false);
+    } else {
+      for (int v = 0; v < nv; v++)
+        if (!reason[v]) reason[v] = -3;
+    }
   }
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double t_solve = now_ms() - ts0;

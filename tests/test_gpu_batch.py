@@ -68,3 +68,23 @@ def test_batch_schedule_cache_and_errors():
     with pytest.raises(PrbfError) as e:
         batch_interpolate(probs, max_it=2)
     assert e.value.status == 5  # not converged
+
+
+def test_mixed_batch_meets_the_fp64_residual_and_routes_ill_conditioned_problems():
+    # FP32 sums and block factors inside FP64 refinement per problem. Jittered lattices with
+    # h/sigma >= 0.72 are well enough conditioned for it; uniform-random points (pairs far
+    # closer than h) and the lattice with h/sigma 0.64 have blocks whose FP32 Cholesky fails
+    # (smallest eigenvalues 1e-7 .. 5e-11), and are solved as an FP64 batch instead
+    lat = W.config4_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
+    probs = lat + _small_batch(3, seed=5)
+    g, its, reason, st = batch_interpolate(probs, rtol=1e-13, pc="asm", precision="mixed")
+    assert st.nconverged == len(probs) and all(r > 0 for r in reason)
+    assert 4 <= st.nprob_fp64 <= len(probs) - 2
+    assert st.outer_its >= 2 and st.t_matvec32_ms > 0
+    assert st.max_true_rel_resid < 1e-10
+    for q, gq in zip(probs, g):
+        assert _true_resid(q, gq) < 1e-10
+    # the well-conditioned lattices meet the refinement's own test, rtol on ||f - A g||
+    for q, gq in zip(lat, g):
+        if q["meta"]["h_over_sigma"] > 0.8:
+            assert _true_resid(q, gq) < 2e-13

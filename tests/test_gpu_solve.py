@@ -131,6 +131,33 @@ def test_solve_config1_mixed_reaches_fp64_answer():
     assert e32 < -11.5 and abs(e32 - e64) < 1.0
 
 
+def test_mixed_falls_back_to_fp64_on_ill_conditioned_points():
+    # uniform-random points: blocks with smallest eigenvalues near 5e-11 (far below FP32's
+    # resolution); the refinement stalls and the call is solved in FP64, to the plain
+    # form's answer. A jittered lattice at h/sigma 0.97 stays in the mixed form.
+    q = W.config4(nprob=1, seed=5, nmin=3000, nmax=4000)[0]
+    args = (q["sigma"], q["nsigma_box"], q["sigma_buffer"], q["sigma_trunc"])
+    kw = dict(sigma=q["sigma"], nsigma_box=q["nsigma_box"], sigma_buffer=q["sigma_buffer"],
+              sigma_trunc=q["sigma_trunc"], pc="asm")
+    with Context(precision="mixed", **kw) as c:
+        gm, sm = c.interpolate(q["x"], q["y"], None, q["f"])
+    with Context(**kw) as c:
+        gd, sd = c.interpolate(q["x"], q["y"], None, q["f"])
+    assert sm.fp64_fallback == 1 and sm.reason == 2 and sd.fp64_fallback == 0
+    assert sm.its >= sd.its
+    np.testing.assert_array_equal(gm, gd)  # the same FP64 solve from zero
+    gr = O.grid_for(q["x"], q["y"], None, *args)
+    perm, cs = O.cell_sort(gr, q["x"], q["y"])
+    r = O.matvec(gr, q["x"][perm], q["y"][perm], None, cs, gm[perm]) - q["f"][perm]
+    assert np.linalg.norm(r) / np.linalg.norm(q["f"]) < 1e-10
+    lat = [p for p in W.config4_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
+           if p["meta"]["h_over_sigma"] > 0.95][0]
+    with Context(precision="mixed", sigma=lat["sigma"], nsigma_box=lat["nsigma_box"],
+                 sigma_buffer=lat["sigma_buffer"], sigma_trunc=lat["sigma_trunc"], pc="asm") as c:
+        _, sl = c.interpolate(lat["x"], lat["y"], None, lat["f"])
+    assert sl.fp64_fallback == 0 and sl.reason == 2 and sl.true_rel_resid <= 1e-13
+
+
 def test_solve_jittered_and_multiple_rhs():
     p = W.lamb_oseen_2d(50, jitter=0.25, seed=8)
     f2 = np.stack([p.f, np.cos(3 * p.x) * np.sin(2 * p.y)], axis=1)
