@@ -207,6 +207,26 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
                           float* wg, int np, float* xp, float* yp, float* zp, float* gp,
                           float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc);
 
+/* The reference's C++ -> CUDA seam gpumatmult (2d/gpumatmult.cu:65-67; 3d/gpumatmult.cu:73-75),
+ * same argument meaning, for callers that keep the reference's host packer
+ * (2d/matmultgpu.cxx:9-97): iblok blocks of 128 FP32 target slots (tX, tY[, tZ]; slots past a
+ * cell's points zero-padded), the blocks' truncation sets packed one after the other
+ * (sX, sY[, sZ], sG; block b's at offset[b] .. offset[b+1]-1, iblok + 1 offsets), sigma, and
+ * the capacities the caller allocated (numCluster*128 target slots, numCluster*numTrunc
+ * sources; iblok <= numCluster, offset[iblok] <= numCluster*numTrunc). Writes
+ * tW[128 b + i] = sum_j sG_j exp(-|t - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2) for the
+ * 128 * iblok slots (the 3D form keeps this 2D normalisation, as the reference's does).
+ * FP32 arithmetic on the caller's coordinates. Host pointers; the call is synchronous and
+ * returns a PRBF_* status (the reference's returns void and checks nothing). Device
+ * buffers are grow-only and kept per device for the life of the process, as the
+ * reference's statics are; concurrent calls are serialised. */
+int prbf_gpumatmult_2d(const float* tX, const float* tY, float* tW, const float* sX, const float* sY,
+                       const float* sG, const int* offset, int iblok, float sigma, int numCluster,
+                       int numTrunc);
+int prbf_gpumatmult_3d(const float* tX, const float* tY, const float* tZ, float* tW, const float* sX,
+                       const float* sY, const float* sZ, const float* sG, const int* offset, int iblok,
+                       float sigma, int numCluster, int numTrunc);
+
 /* Cell sort that allocates nothing (no counterpart in the reference). For callers that
  * must not allocate device memory themselves -- an application that reserves the whole
  * GPU for its own memory pool, or a latency-critical loop that cannot afford the device

@@ -231,6 +231,34 @@ def RBFInterpolation(xg, yg, zg, wg, xp, yp, zp, gp, sigma, nsigma_box, sigma_bu
                                          int(sigma_trunc))
 
 
+def gpumatmult(tx, ty, tz, sx, sy, sz, sg, offset, sigma, num_cluster=None, num_trunc=None):
+    """The reference's GPU seam (2d/gpumatmult.cu:65-67; 3d/gpumatmult.cu:73-75) on packed
+    FP32 arrays: tx, ty(, tz) hold iblok blocks of 128 target slots, sx, sy(, sz), sg the
+    blocks' truncation sets one after the other, offset the iblok + 1 block starts (tz and
+    sz None in 2D). num_cluster / num_trunc default to the tightest capacities. Returns tw
+    (128 * iblok FP32 values)."""
+    f32 = lambda a: np.ascontiguousarray(a, np.float32) if a is not None else None
+    tx, ty, tz, sx, sy, sz, sg = (f32(a) for a in (tx, ty, tz, sx, sy, sz, sg))
+    off = np.ascontiguousarray(offset, np.int32)
+    iblok = len(off) - 1
+    if iblok < 0 or len(tx) != 128 * iblok:
+        raise ValueError("targets must hold 128 slots per block and offset iblok + 1 entries")
+    ncl = iblok if num_cluster is None else int(num_cluster)
+    ntr = (max(1, -(-int(off[-1]) // max(ncl, 1))) if iblok else 0) if num_trunc is None else int(num_trunc)
+    tw = np.zeros(128 * iblok, np.float32)
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    ip = off.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    if tz is None:
+        code = N.lib().prbf_gpumatmult_2d(fp(tx), fp(ty), fp(tw), fp(sx), fp(sy), fp(sg), ip, iblok,
+                                          float(sigma), ncl, ntr)
+    else:
+        code = N.lib().prbf_gpumatmult_3d(fp(tx), fp(ty), fp(tz), fp(tw), fp(sx), fp(sy), fp(sz), fp(sg), ip,
+                                          iblok, float(sigma), ncl, ntr)
+    if code:
+        raise PrbfError(code, "prbf_gpumatmult")
+    return tw
+
+
 def vorticity_evaluation(xi, yi, *args, **opts):
     """vorticity_evaluation(xi, yi, [zi,] xj, yj, [zj,] gj, sigma, nsigma_box,
     sigma_buffer, sigma_trunc) -> wi: the interpolant with weights gj at sources

@@ -39,3 +39,23 @@ def test_status_strings_and_defaults():
     assert p.dim == 2 and p.restart == 30 and p.rtol == 1e-13 and p.max_it == 1000
     assert L.prbf_status_string(0) == b"ok"
     assert L.prbf_status_string(N.ERR_STATE) == b"call out of order"
+
+
+def test_gpumatmult_argument_checks_need_no_gpu():
+    # the seam validates its arguments before any CUDA call
+    import numpy as np
+    from petrbf_gb300 import _native as N
+    L = N.lib()
+    f = np.zeros(256, np.float32)
+    fp = f.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    ok = np.array([0, 3, 5], np.int32)
+    bad = np.array([0, 3, 2], np.int32)
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    call = lambda off, iblok, ncl, ntr, sigma=0.1: L.prbf_gpumatmult_2d(fp, fp, fp, fp, fp, fp, ip(off), iblok,
+                                                                       sigma, ncl, ntr)
+    assert call(ok, 0, 2, 3) == N.OK                 # nothing to do
+    assert call(ok, 2, 1, 3) == N.ERR_ARG            # more blocks than the capacity
+    assert call(bad, 2, 2, 3) == N.ERR_ARG           # decreasing offsets
+    assert call(ok, 2, 2, 2) == N.ERR_CAPACITY       # 5 sources > 2 x 2
+    assert call(ok, 2, 2, 3, sigma=0.0) == N.ERR_ARG
+    assert L.prbf_gpumatmult_3d(fp, fp, None, fp, fp, fp, fp, fp, ip(ok), 2, 0.1, 2, 3) == N.ERR_ARG
