@@ -188,12 +188,15 @@ struct Chunk {
   }
 };
 
-// acc[4][4] -= sum_m As[m][r] Bs[m][c] over the staged chunk
+// acc[4][4] -= sum_m As[m][r] Bs[m][c] over the first mm entries of the staged chunk.
+// Rows at or past nr (the tile's height) are zero padding that is never stored: their
+// threads skip the arithmetic, whole warps where the tile ends above their 8 rows (the
+// short last tile of a block), and a partial chunk stops at mm.
 template <class T>
-__device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4], int ty, int tx) {
+__device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4], int ty, int tx, int nr, int mm) {
+  if (4 * ty >= nr) return;
   constexpr int S = SP<T>::S;
-#pragma unroll
-  for (int m = 0; m < KCOf<T>::v; m++) {
+  auto step = [&](int m) {
     T a[4], b[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -204,6 +207,13 @@ __device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4],
     for (int p = 0; p < 4; p++)
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[p][q] = fma(-a[p], b[q], acc[p][q]);
+  };
+  if (mm == KCOf<T>::v) {
+#pragma unroll
+    for (int m = 0; m < KCOf<T>::v; m++) step(m);
+  } else {
+#pragma unroll 4
+    for (int m = 0; m < mm; m++) step(m);
   }
 }
 
@@ -238,7 +248,7 @@ __device__ void tile_update(Tiles<T>& t, T acc[4][4], const T* P, long long ldp,
     cb.store(Bs, tb);
     __syncthreads();
     if (c + 1 < nchunk) fetch((c + 1) * KC);  // in flight during this chunk's arithmetic
-    mma_chunk<T>(As, Bs, acc, ty, tx);
+    mma_chunk<T>(As, Bs, acc, ty, tx, nr, min(KC, nm - c * KC));
   }
 }
 
