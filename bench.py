@@ -553,6 +553,8 @@ def run_case(name):
             c.pc_apply(r)
     elif name == "batch":  # 24 problems of the batched form (N up to 6x10^4)
         batch_interpolate(W.config4(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
+    elif name == "batch_mixed":  # 24 jittered-lattice problems of the batched form, mixed
+        batch_interpolate(W.config4_lattice(nprob=24, nmax=60000), rtol=1e-13, pc="asm", precision="mixed")
     elif name == "seam_2d":  # the gpumatmult seam on the packed arrays of a 10^6-point lattice
         run_seam_case()
         return
