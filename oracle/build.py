@@ -8,6 +8,10 @@
   stand-in in ``oracle/ref_stub``. Only built where the reference tree is present; it
   generates the golden fixtures under tests/golden and is never shipped or linked by
   the product.
+* ``oracle/_ref/gpumatmult_2d.cubin`` / ``_3d.cubin``: the reference's own FP32 GPU kernel
+  (2d/gpumatmult.cu, 3d/gpumatmult.cu), device code compiled unmodified for sm_103a where
+  the reference tree is present; ``oracle/refgpu.py`` loads it through the CUDA driver API
+  for the seam's parity test.
 """
 import os
 import subprocess
@@ -56,6 +60,13 @@ def build_ref(ref_root, force=False):
             _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
                   "-DREF_DIM=%d" % dim, "-I", stub, "-I", tree, "-o", out] + srcs)
         outs.append(out)
+        # the reference's own FP32 GPU kernel (gpumatmult.cu), device code only, unmodified
+        cu = os.path.join(tree, "gpumatmult.cu")
+        cub = os.path.join(HERE, "_ref", "gpumatmult_%dd.cubin" % dim)
+        if os.path.exists(cu) and (force or _stale(cub, [cu])):
+            _run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w", "-o", cub, cu])
+        if os.path.exists(cub):
+            outs.append(cub)
     return outs
 
 

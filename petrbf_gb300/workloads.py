@@ -197,6 +197,42 @@ def config4_lattice(nprob=256, seed=2025, nmin=2000, nmax=200000, nsigma_box=4):
     return out
 
 
+def pack_gpumatmult_2d(m=1000, seed=1):
+    """Packs a jittered m x m lattice the way the reference's host packer does
+    (2d/matmultgpu.cxx:39-71) for the config-2 geometry (cell 8 sigma, sources of a cell =
+    the points of its 3 x 3 cells, which the 12 sigma truncation box spans): 128 FP32
+    target slots per cell, the cells' source sets one after the other, CSR offsets."""
+    x, y, h = lattice_2d(m, jitter=0.25, seed=seed)
+    sigma = h / 0.8
+    box = 8 * sigma + 1e-6
+    x0, y0 = x.min() - 1e-6, y.min() - 1e-6
+    nx, ny = int(np.ceil((x.max() + 1e-6 - x0) / box)), int(np.ceil((y.max() + 1e-6 - y0) / box))
+    ix = np.minimum(((x - x0) / box).astype(np.int64), nx - 1)
+    iy = np.minimum(((y - y0) / box).astype(np.int64), ny - 1)
+    cell = ix * ny + iy
+    order = np.argsort(cell, kind="stable")
+    cs = np.zeros(nx * ny + 1, np.int64)
+    np.cumsum(np.bincount(cell, minlength=nx * ny), out=cs[1:])
+    xs, ys = x[order].astype(np.float32), y[order].astype(np.float32)
+    gs = np.random.default_rng(seed).standard_normal(len(x)).astype(np.float32)
+    tx = np.zeros(128 * nx * ny, np.float32)
+    ty = np.zeros_like(tx)
+    src, off = [], [0]
+    for cx in range(nx):
+        for cy in range(ny):
+            c = cx * ny + cy
+            a, b = cs[c], cs[c + 1]
+            assert b - a <= 128
+            tx[128 * c:128 * c + b - a] = xs[a:b]
+            ty[128 * c:128 * c + b - a] = ys[a:b]
+            idx = np.concatenate([np.arange(cs[jx * ny + max(cy - 1, 0)], cs[jx * ny + min(cy + 1, ny - 1) + 1])
+                                  for jx in range(max(cx - 1, 0), min(cx + 1, nx - 1) + 1)])
+            src.append(idx)
+            off.append(off[-1] + len(idx))
+    idx = np.concatenate(src)
+    return tx, ty, xs[idx], ys[idx], gs[idx], np.array(off, np.int32), np.float32(sigma), int(cs[-1])
+
+
 def log10_rel_error(w, e):
     """log10(||w - e||_2 / ||e||_2), 2d/main.cxx:130-133."""
     w = np.asarray(w, np.float64)

@@ -94,3 +94,44 @@ def test_gpumatmult_long_sets_and_empty_blocks():
     we, mag = _expected(2, float(sigma), [tx, ty], [sx, sy, sg], off)
     assert np.all(np.abs(tw - we) <= 1e-5 * mag + 1e-30)
     assert np.all(tw[128:256] == 0)
+
+
+def _ref_kernel(dim):
+    from oracle import refgpu
+    if not refgpu.available(dim):
+        pytest.skip("the reference's gpumatmult.cu is compiled only where the reference tree is (oracle/_ref)")
+    return refgpu.RefKernel(dim)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gpumatmult_matches_the_reference_kernel(golden, case):
+    # the reference's own kernel (2d/gpumatmult.cu:20-63, 3d:22-71, compiled unmodified) on
+    # the same packed arrays: both FP32, within 2e-5 of the sum of |terms| of each slot
+    d = golden(case)
+    dim, sigma, g, T, S, off, slots = _pack(d)
+    ref = _ref_kernel(dim)
+    tr = ref(T, S, off, np.float32(sigma))
+    tw = gpumatmult(T[0], T[1], T[2] if dim == 3 else None, S[0], S[1], S[2] if dim == 3 else None,
+                    S[dim], off, np.float32(sigma))
+    we, mag = _expected(dim, sigma, T, S, off)
+    assert np.all(np.abs(tr - we) <= 2e-5 * mag + 1e-30)  # the reference kernel itself
+    assert np.all(np.abs(tw - tr) <= 2e-5 * mag + 1e-30)
+
+
+def test_gpumatmult_and_reference_kernel_on_a_million_points():
+    # 10^6-point lattice packed as the reference's packer packs it (10,000 blocks, 8.9e6
+    # sources): the two kernels agree; each runs three times so that a launch list of this
+    # test shows both kernels' device times side by side
+    from petrbf_gb300.workloads import pack_gpumatmult_2d
+    tx, ty, sx, sy, sg, off, sigma, npts = pack_gpumatmult_2d()
+    ref = _ref_kernel(2)
+    args = ref.device_args([tx, ty], [sx, sy, sg], off, sigma)
+    for _ in range(3):
+        ref.launch(*args)
+    import torch
+    torch.cuda.synchronize()
+    tr = args[3].cpu().numpy()
+    for _ in range(3):
+        tw = gpumatmult(tx, ty, None, sx, sy, None, sg, off, sigma)
+    scale = np.max(np.abs(tr))
+    assert np.max(np.abs(tw - tr)) <= 1e-4 * scale
