@@ -306,3 +306,35 @@ def test_cdata_cylinder_matches_oracle(golden):
     # error metric of the cylinder driver (2d/cylinder.cxx:123-127): residual level
     err = W.log10_rel_error(w, p.f)
     assert err < -13.0 and abs(err - float(d["solve_log10_err"][0])) < 0.5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_edge_point_sets(precision):
+    kw = dict(nsigma_box=8, sigma_buffer=24, sigma_trunc=24, precision=precision)
+    # one point: g = f 2 pi sigma^2
+    with Context(sigma=0.025, **kw) as c:
+        g, st = c.interpolate(np.array([0.3]), np.array([-0.2]), None, np.array([1.5]))
+    assert st.reason == 2 and abs(g[0] - 1.5 * 2 * np.pi * 0.025 ** 2) <= 1e-13 * g[0]
+    # collinear points (a degenerate bounding box: one row of cells)
+    xl = np.linspace(-1, 1, 1000)
+    with Context(sigma=2.0 / 999 / 0.8, **kw) as c:
+        g, st = c.interpolate(xl, np.zeros(1000), None, np.exp(-xl ** 2))
+    assert st.reason == 2 and st.true_rel_resid < 1e-13
+    # collisions: five points repeated with the same value -- singular blocks (the reference's
+    # PETSc LU stops on the zero pivot); the blocks are factored with a diagonal shift and the
+    # consistent system is still solved to the tolerance (the mixed form hands it to FP64)
+    p = W.config1()
+    idx = np.arange(10, 15)
+    x, y = np.concatenate([p.x, p.x[idx]]), np.concatenate([p.y, p.y[idx]])
+    f = np.concatenate([p.f, p.f[idx]])
+    with _ctx(p, precision=precision) as c:
+        g, st = c.interpolate(x, y, None, f)
+    assert st.reason == 2 and st.nblocks_fallback > 0 and st.true_rel_resid < 1e-12
+    assert st.fp64_fallback == (1 if precision == "mixed" else 0)
+    # ... and with different values at the same point there is no solution: a clean error
+    f2 = f.copy()
+    f2[-5:] += 0.1
+    with _ctx(p, precision=precision, max_it=200) as c:
+        with pytest.raises(PrbfError) as e:
+            c.interpolate(x, y, None, f2)
+    assert e.value.status == 5  # PRBF_ERR_NOT_CONVERGED
