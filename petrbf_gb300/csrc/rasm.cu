@@ -94,16 +94,29 @@ __global__ void k_buffer_lists(Grid g, const double* __restrict__ x, const doubl
 }
 
 // ---- block assembly ----------------------------------------------------------------
+// FP32 form: every coordinate as an unevaluated sum of two floats, v = h + l (h = v
+// rounded, l = the rest rounded), so that a difference is (h_a - h_b) + (l_a - l_b) in FP32
+// (within 1.5 ulp of the exact difference, as against 0.5 ulp for an FP64 difference
+// rounded once) without the FP64 pipe.
+__global__ void k_split_hl(long long n, const double* __restrict__ v, float2* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = v[i];
+    const float h = (float)a;
+    out[i] = make_float2(h, (float)(a - (double)h));
+  }
+}
+
 // K[i][j] = exp(-|x_a - x_b|^2 / (2 sigma^2)) (+ shift on the diagonal), block order
 // neighbours first then centre: block row i < n1 -> buffer entry nc + i, else i - n1.
-// Lower triangle only (the factorisation reads nothing else).
+// Lower triangle only (the factorisation reads nothing else). hl (FP32 form): the n
+// points' coordinates split by k_split_hl, dim arrays of n one after the other.
 template <class T>
 __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const long long* __restrict__ boff,
                            const int* __restrict__ cs, const int* __restrict__ idx,
                            const long long* __restrict__ koff, const double* __restrict__ x,
                            const double* __restrict__ y, const double* __restrict__ z, int dim, double inv2s2_all,
                            const double* __restrict__ cell_sig, double shift, T* __restrict__ K,
-                           const unsigned char* __restrict__ only) {
+                           const unsigned char* __restrict__ only, const float2* __restrict__ hl, long long n) {
   int b = blockIdx.y;
   if (b >= nblk || (only && !only[b])) return;
   int c = blk_cell[b];
@@ -115,17 +128,21 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
   for (int i = blockIdx.x; i < nbk; i += gridDim.x) {
     const int pa = id[i < n1 ? nc + i : i - n1];
     const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
+    float2 ha[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    if constexpr (std::is_same<T, float>::value)
+      for (int d = 0; d < dim; d++) ha[d] = hl[d * n + pa];
+    const float c2 = (float)(inv2s2 * 1.4426950408889634);
     for (int j = threadIdx.x; j <= i; j += blockDim.x) {
       const int pb = id[j < n1 ? nc + j : j - n1];
       if constexpr (std::is_same<T, float>::value) {
-        // differences in FP64 (coordinates are absolute), exponent in FP32 (SFU exp2)
-        float dx = (float)(xa - x[pb]), dy = (float)(ya - y[pb]);
-        float r2 = dx * dx + dy * dy;
-        if (dim == 3) {
-          float dz = (float)(za - z[pb]);
-          r2 = fmaf(dz, dz, r2);
+        // differences of the split coordinates in FP32, exponent in FP32 (SFU exp2)
+        float r2 = 0.f;
+        for (int d = 0; d < dim; d++) {
+          const float2 hb = hl[d * n + pb];
+          const float dd = (ha[d].x - hb.x) + (ha[d].y - hb.y);
+          r2 = fmaf(dd, dd, r2);
         }
-        float v = exp2f(-r2 * (float)(inv2s2 * 1.4426950408889634));
+        float v = exp2f(-r2 * c2);
         if (i == j) v += (float)shift;
         A[(long long)i * nbk + j] = v;
       } else {
@@ -1230,6 +1247,16 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   R.nfallback = 0;
   R.retried.clear();
+  // FP32 form: the coordinates split into float pairs once (the assembly then stays on the
+  // FP32 pipes)
+  float2* hl = nullptr;
+  if (fp32) {
+    hl = (float2*)ws.get(55, sizeof(float2) * (size_t)G.dim * std::max(G.n, 1));
+    const double* xyz[3] = {G.x, G.y, G.z};
+    const int gb = (int)std::max<long long>(1, std::min<long long>(((long long)G.n + 255) / 256, 8 * 152));
+    for (int d = 0; d < G.dim; d++) k_split_hl<<<gb, 256, 0, s>>>(G.n, xyz[d], hl + (size_t)d * G.n);
+    PRBF_CHECK_LAUNCH();
+  }
   size_t pos = 0;
   std::vector<long long> hk, hx;
   std::vector<int> bc;
@@ -1270,7 +1297,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       dim3 ag(64, nb_batch);
       if (fp32) {
         k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
-                                             inv2s2, G.cell_sigma, shift, (float*)Kw, only);
+                                             inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n);
         PRBF_CHECK_LAUNCH();
         // the Cholesky on the tensor cores, then the factor / S_c epilogues of k_chol_sc
         k_chol_tc<<<nb_batch, NTH, chol_tc_smem(), s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
@@ -1286,7 +1313,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
                                                        G.cell_sigma, dbad, only, 0, nullptr, nullptr, 1);
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
-                                              G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only);
+                                              G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only, nullptr, 0);
         PRBF_CHECK_LAUNCH();
         k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (double*)Kw, dx,
                                                       (double*)Xw, R.soff.get(), nullptr,
