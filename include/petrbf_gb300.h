@@ -115,6 +115,12 @@ const char* prbf_last_error(const prbf_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
 void* prbf_ctx_stream(prbf_ctx* ctx);
 int prbf_ctx_synchronize(prbf_ctx* ctx);
+/* Self-test of the failure path of the kernels' bounded waits (no counterpart in the
+ * reference): a one-warp kernel polls, max_polls times (1 .. 2^20), an mbarrier that
+ * nothing completes, raises the device error word and the call returns PRBF_ERR_TIMEOUT,
+ * as any library call does when a kernel's copy or MMA wait gives up. The context stays
+ * usable. */
+int prbf_selftest_wait_timeout(prbf_ctx* ctx, unsigned max_polls);
 
 /* rbf_interpolation: weights g with A g = f for n points; nrhs right-hand sides stored
  * one after the other (f[r*n + i]); weights written the same way, in the caller's order.

@@ -110,6 +110,7 @@ SIGNATURES = {
     "prbf_RBFInterpolation": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, _F, _F, _F,
                                              _F, ctypes.c_int, _F, _F, _F, _F, ctypes.c_float,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "prbf_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint]),
     "prbf_gpumatmult_2d": (ctypes.c_int, [_F, _F, _F, _F, _F, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                           ctypes.c_float, ctypes.c_int, ctypes.c_int]),
     "prbf_gpumatmult_3d": (ctypes.c_int, [_F, _F, _F, _F, _F, _F, _F, _F, ctypes.POINTER(ctypes.c_int),

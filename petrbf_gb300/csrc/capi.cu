@@ -132,6 +132,22 @@ void upload_coords(Ctx& c, int n, const double* x, const double* y, const double
 
 }  // namespace
 
+namespace prbf {
+namespace {
+// A wait that nothing completes: one warp initialises an mbarrier that expects one arrival
+// which never comes, polls it max_polls times with the bounded wait of the kernels, and
+// raises DEV_ERR_TIMEOUT -- the path a lost copy or MMA completion takes, run without
+// leaving anything behind (no copy or MMA is in flight, the barrier dies with the CTA).
+__global__ void k_selftest_wait(unsigned max_polls, unsigned* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  const bool done = mbar_wait(&bar, 0, max_polls);
+  if (!done && threadIdx.x == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+}
+}  // namespace
+}  // namespace prbf
+
 extern "C" {
 
 void prbf_params_default(prbf_params* p) {
@@ -211,6 +227,15 @@ void* prbf_ctx_stream(prbf_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullp
 
 int prbf_ctx_synchronize(prbf_ctx* ctx) {
   return guarded(ctx, [&](Ctx& c) { PRBF_CUDA(cudaStreamSynchronize(c.stream)); });
+}
+
+int prbf_selftest_wait_timeout(prbf_ctx* ctx, unsigned max_polls) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (max_polls == 0 || max_polls > (1u << 20)) throw Error(PRBF_ERR_ARG, "max_polls must be in [1, 2^20]");
+    k_selftest_wait<<<1, 32, 0, c.stream>>>(max_polls, c.err.get());
+    PRBF_CHECK_LAUNCH();
+    c.check_device_error("self-test wait");
+  });
 }
 
 int prbf_matvec_setup(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z) {

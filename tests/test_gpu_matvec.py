@@ -148,3 +148,17 @@ def test_errors_are_reported():
         with pytest.raises(PrbfError) as e:
             c.matvec_setup(np.array([0.0, np.nan]), np.array([0.0, 1.0]))
         assert e.value.status == 2  # PRBF_ERR_RANGE
+
+
+def test_bounded_wait_timeout_is_reported_and_the_context_survives():
+    # the failure path of the kernels' bounded mbarrier waits, made to run out on purpose by
+    # a wait that nothing completes (no copy or MMA in flight): PRBF_ERR_TIMEOUT, then the
+    # same context computes correctly
+    from petrbf_gb300 import _native as N
+    with Context(dim=2, sigma=0.1) as c:
+        assert N.lib().prbf_selftest_wait_timeout(c.h, 256) == N.ERR_TIMEOUT
+        assert "gave up" in N.lib().prbf_last_error(c.h).decode()
+        assert N.lib().prbf_selftest_wait_timeout(c.h, 0) == N.ERR_ARG
+        c.matvec_setup(np.array([0.3]), np.array([-0.2]))
+        y = c.matvec(np.array([2.0]))
+        assert abs(y[0] - 2.0 / (2 * np.pi * 0.01)) < 1e-12 * y[0]
