@@ -162,3 +162,31 @@ def test_bounded_wait_timeout_is_reported_and_the_context_survives():
         c.matvec_setup(np.array([0.3]), np.array([-0.2]))
         y = c.matvec(np.array([2.0]))
         assert abs(y[0] - 2.0 / (2 * np.pi * 0.01)) < 1e-12 * y[0]
+
+
+@pytest.mark.parametrize("which", ["config2", "config3"])
+def test_full_size_matvec_rows_against_oracle(which):
+    # the full-size workloads (4x10^6 points in 2D, 128^3 in 3D): 2000 sampled rows of the
+    # GPU's FP64 sum against the oracle's evaluation of the same sum at those points, and
+    # the FP32 sum's rows within its own tolerance
+    p = getattr(W, which)()
+    z = p.z if p.dim == 3 else None
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(p.n)
+    import torch
+    with Context(dim=p.dim, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+                 sigma_trunc=p.sigma_trunc) as c:
+        c.matvec_setup(p.x, p.y, z)
+        y = c.matvec(v)
+        vt = torch.from_numpy(v).cuda()
+        ot = torch.empty_like(vt)
+        torch.cuda.synchronize()
+        c.matvec_dev(vt.data_ptr(), ot.data_ptr(), cell_order=False, fp32=True)
+        c.synchronize()
+        y32 = ot.cpu().numpy()
+    k = rng.choice(p.n, 2000, replace=False)
+    zk = z[k] if z is not None else None
+    yo = O.vorticity_evaluation(p.x[k], p.y[k], zk, p.x, p.y, z, v, *p.params())
+    scale = np.max(np.abs(yo))
+    assert np.max(np.abs(y[k] - yo)) <= 1e-12 * scale
+    assert np.max(np.abs(y32[k] - yo)) <= 1e-4 * scale
