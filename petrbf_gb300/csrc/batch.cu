@@ -253,7 +253,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
     // truncation-set sizes (the per-problem plan) and buffer-list sizes
     GaussPlan lp;
     lp.g = P.g;
-    gauss_plan_dev(lp, P.view(), P.view(), c.err.get(), c.ws, c.stream);
+    gauss_plan_dev(lp, P.view(), P.view(), c.err.get(), c.ws, c.stream, false);
     PRBF_CUDA(cudaMemcpyAsync(B.trunc.get() + co, lp.trunc_cnt.get(), sizeof(int) * nc, cudaMemcpyDeviceToDevice,
                               c.stream));
     pairs += lp.pairs;

@@ -100,11 +100,21 @@ struct GaussPlan {
   long long g32_stride = 0;
   DevBuf<float> su, sv, sw, g32;
   DevBuf<unsigned long long> smask;
+  // FP64 matvec with each exponential used for both rows (targets == sources, every cell
+  // <= 128 points): K partial slots of pstride entries (kept zero between products) and
+  // each point's cell y index
+  bool sym_ready = false;
+  int sym_K = 0;
+  long long sym_pstride = 0;
+  DevBuf<double> sym_part;
+  DevBuf<unsigned long long> sym_cy;
 };
 
-// Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc.
+// Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc. forms:
+// also the FP32 form's source data and the symmetric FP64 form's buffers (a plan used only
+// for its sizes passes false).
 void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src,
-                    unsigned* err, Workspace& ws, cudaStream_t s);
+                    unsigned* err, Workspace& ws, cudaStream_t s, bool forms = true);
 // FP32 form's source data of a batch (each problem with its own grid and scale, grids with
 // their first global cell); sets plan.f32_ready when every grid qualifies.
 void gauss_plan_f32_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src, cudaStream_t s);

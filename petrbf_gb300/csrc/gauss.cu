@@ -729,6 +729,435 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
   }
 }
 
+// ---- FP64 matvec with each exponential used for both rows --------------------------
+// When the targets are the sources (the matvec of the solve), the pair (i, j) enters row i
+// when j is in T(c(i)) and row j when i is in T(c(j)), with the same exponential. One CTA
+// per cell c1 (at most kTileT points): its own points against themselves (row i only:
+// the centre cell is taken unconditionally), then against the points of the upper half of
+// its neighbour window -- the window cells with a larger cell index -- computing each
+// exponential once and adding it to row i when j is in T(c1) (the FP64 box test against
+// c1's centre, as the reference's) and to row j when i is in T(c(j)) (the target's box-test
+// bits against the centres of the cells around its own, same arithmetic). Row j's share
+// goes to the partial slot part[o][j], o the window offset of c(j) from c1 -- each slot is
+// written by one CTA only -- and k_sym_gather adds the slots to the rows in a fixed order,
+// zeroing them for the next product. Two ordered pairs cost 12 FP64 instructions in 2D
+// (distance 4, exponential 6, two accumulations) against 2 x 11.
+// Lanes own sources (kSymM at a time), each warp walks all targets in groups of kGroup, and
+// the per-target sums go to per-warp rows of shared memory that are added in warp order
+// at the end: the result does not depend on scheduling.
+constexpr int kSymRC = 512;   // staged sources per fill
+constexpr int kSymKC = 1024;  // compacted sources
+constexpr int kSymM = 2;      // sources per lane at a time
+
+template <int DIM>
+struct LayoutS {
+  static constexpr int NA = DIM + 2;  // staged arrays: coordinates, weight, cell-y word
+  using ET = ExpTab<DIM == 2>;        // 2D: the 1024-entry table (one weight vector)
+  static constexpr size_t raw = 0;                                                     // NA x RC
+  static constexpr size_t comp = align16(raw + sizeof(double) * NA * kSymRC);           // (DIM+1) x KC
+  static constexpr size_t code = align16(comp + sizeof(double) * (DIM + 1) * kSymKC);   // KC
+  static constexpr size_t jidx = align16(code + sizeof(int) * kSymKC);                  // KC
+  static constexpr size_t tgt = align16(jidx + sizeof(int) * kSymKC);                   // (DIM+1) x kTileT
+  static constexpr size_t tmask = align16(tgt + sizeof(double) * (DIM + 1) * kTileT);   // kTileT
+  static constexpr size_t acct = align16(tmask + sizeof(unsigned long long) * kTileT);  // kWarps x kTileT
+  static constexpr size_t tab = align16(acct + sizeof(double) * kWarps * kTileT);
+  static constexpr size_t pieces = align16(tab + sizeof(double) * ET::poly * ET::n);
+  static constexpr size_t prange = align16(pieces + sizeof(Piece) * kMaxPieces);
+  static constexpr size_t bar = align16(prange + sizeof(int) * kMaxPieces);
+  static constexpr size_t total = bar + 16;
+};
+
+// Range r of c1's walk: 0 = c1 itself; 1 = the cells above c1 in its column; then the
+// columns to its right (jy0 .. jy1) in its plane; then (3D) every column of the planes
+// above. Sorted positions [a, b), cell offsets dx, dz from c1.
+__device__ __forceinline__ void sym_range(const Grid& g, const int* __restrict__ cs, int r, int c1, int ix, int iy,
+                                          int iz, int jx0, int jx1, int jy0, int jy1, int& a, int& b, int& dx,
+                                          int& dz) {
+  const int cb = g.cbase;
+  if (r == 0) {
+    a = cs[c1];
+    b = cs[c1 + 1];
+    dx = dz = 0;
+    return;
+  }
+  int cx, cz, y0;
+  if (r == 1) {
+    cx = ix;
+    cz = iz;
+    y0 = iy + 1;
+  } else {
+    const int r2 = r - 2, right = jx1 - ix;
+    y0 = jy0;
+    if (r2 < right) {
+      cx = ix + 1 + r2;
+      cz = iz;
+    } else {
+      const int ncolx = jx1 - jx0 + 1, r3 = r2 - right;
+      cz = iz + 1 + r3 / ncolx;
+      cx = jx0 + r3 % ncolx;
+    }
+  }
+  dx = cx - ix;
+  dz = cz - iz;
+  if (y0 > jy1) {
+    a = b = 0;
+    return;
+  }
+  a = cs[cb + cell_of(g, cx, y0, cz)];
+  b = cs[cb + cell_of(g, cx, jy1, cz) + 1];
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_gauss_sym(
+    Grid g, const int2* __restrict__ items, int nitems, const double* __restrict__ sx,
+    const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
+    const unsigned long long* __restrict__ pcy, const int* __restrict__ cs, double* __restrict__ w,
+    double* __restrict__ part, long long pstride, SumConsts kc, unsigned* err, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  using Lay = LayoutS<DIM>;
+  using ET = typename Lay::ET;
+  constexpr int NA = Lay::NA, RC = kSymRC, KC = kSymKC;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* raw = (double*)(smem + Lay::raw);
+  double* comp = (double*)(smem + Lay::comp);
+  int* ccode = (int*)(smem + Lay::code);
+  int* cj = (int*)(smem + Lay::jidx);
+  double* tgt = (double*)(smem + Lay::tgt);
+  unsigned long long* tmk = (unsigned long long*)(smem + Lay::tmask);
+  double* acct = (double*)(smem + Lay::acct);
+  double* tab = (double*)(smem + Lay::tab);
+  Piece* pieces = (Piece*)(smem + Lay::pieces);
+  int* prange = (int*)(smem + Lay::prange);
+  uint64_t* bar = (uint64_t*)(smem + Lay::bar);
+  __shared__ int s_wsum[kWarps];
+  __shared__ int s_fill[3];
+  __shared__ int s_cursor[2];
+  __shared__ int s_abort;
+  __shared__ unsigned long long s_tor;
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (DIM == 2 ? d_tab_big : d_tab_small)[i];
+  if (tid == 0) mbar_init(bar, 1);
+  unsigned phase = 0;
+  const int G = gridDim.x;
+  const int nb = g.nb_trunc, W = 2 * nb + 1;
+  const double L = g.trunc_len, kexp = kc.kexp;
+
+  for (int round = 0; (long long)round * G < nitems; round++) {
+    const int it = (round & 1) ? round * G + (G - 1 - (int)blockIdx.x) : round * G + (int)blockIdx.x;
+    if (it >= nitems) continue;
+    const int c1 = items[it].x, t0 = items[it].y;
+    const int nt = min(kTileT, cs[c1 + 1] - t0);  // every cell has at most kTileT points here
+    int ix, iy, iz;
+    cell_xyz(g, c1, ix, iy, iz);
+    const double xc = centre_coord(g.xmin, ix, g.box);
+    const double yc = centre_coord(g.ymin, iy, g.box);
+    const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
+    const int jx0 = max(0, ix - nb), jx1 = min(g.nx - 1, ix + nb);
+    const int jy0 = max(0, iy - nb), jy1 = min(g.ny - 1, iy + nb);
+    const int jz1 = DIM == 3 ? min(g.nz - 1, iz + nb) : iz;
+    const int nranges = 2 + (jx1 - ix) + (DIM == 3 ? (jz1 - iz) * (jx1 - jx0 + 1) : 0);
+
+    __syncthreads();  // the previous item's readers are done
+    if (tid == 0) s_tor = 0ull;
+    __syncthreads();
+    for (int t = tid; t < kTileT; t += kThreads) {
+      double xt = 0.0, yt = 0.0, zt = 0.0, gt = 0.0;
+      unsigned long long m = 0ull;
+      if (t < nt) {
+        xt = sx[t0 + t];
+        yt = sy[t0 + t];
+        if (DIM == 3) zt = sz[t0 + t];
+        gt = sg[t0 + t];
+        // the reference's box test of this point against the centres of the cells at
+        // offsets -nb .. nb of its own (2d/get_trunc.h:63): bit o + nb per axis
+        for (int o = -nb; o <= nb; o++) {
+          if (fabs(xt - centre_coord(g.xmin, ix + o, g.box)) < L) m |= 1ull << (o + nb);
+          if (fabs(yt - centre_coord(g.ymin, iy + o, g.box)) < L) m |= 1ull << (kMaskY + o + nb);
+          if (DIM == 3 && fabs(zt - centre_coord(g.zmin, iz + o, g.box)) < L) m |= 1ull << (kMaskZ + o + nb);
+        }
+        atomicOr(&s_tor, m);
+      }
+      tgt[t] = xt - xc;
+      tgt[kTileT + t] = yt - yc;
+      if (DIM == 3) tgt[2 * kTileT + t] = zt - zc;
+      tgt[DIM * kTileT + t] = gt;  // zero for the padding slots: they add nothing to a row j
+      tmk[t] = m;
+#pragma unroll
+      for (int q = 0; q < kWarps; q++) acct[q * kTileT + t] = 0.0;
+    }
+    if (tid == 0) {
+      s_cursor[0] = 0;
+      s_cursor[1] = -1;
+      s_abort = 0;
+    }
+    __syncthreads();
+    const unsigned long long tor = s_tor;
+
+    int ncomp = 0;
+    const int ngroups = (nt + kGroup - 1) / kGroup;
+    auto flush = [&]() {
+      for (int s0 = wid * 32; s0 < ncomp; s0 += kWarps * 32 * kSymM) {
+        double px[kSymM], py[kSymM], pz[kSymM], pg[kSymM], accs[kSymM];
+        int kx[kSymM], ky[kSymM], kz[kSymM];
+        bool self[kSymM], valid[kSymM];
+#pragma unroll
+        for (int m = 0; m < kSymM; m++) {
+          const int idx = s0 + lane + m * kWarps * 32;
+          valid[m] = idx < ncomp;
+          const int cd = valid[m] ? ccode[idx] : -1;
+          self[m] = cd < 0;
+          kx[m] = cd & 255;
+          ky[m] = kMaskY + ((cd >> 8) & 255);
+          kz[m] = kMaskZ + ((cd >> 16) & 255);
+          px[m] = valid[m] ? comp[idx] : 0.0;
+          py[m] = valid[m] ? comp[KC + idx] : 0.0;
+          pz[m] = (DIM == 3 && valid[m]) ? comp[2 * KC + idx] : 0.0;
+          pg[m] = valid[m] ? comp[DIM * KC + idx] : 0.0;
+          accs[m] = 0.0;
+        }
+        for (int gi = 0; gi < ngroups; gi++) {
+          double tu[kGroup], tv[kGroup], tw[kGroup], tg[kGroup], a[kGroup];
+          unsigned long long tm[kGroup];
+#pragma unroll
+          for (int k = 0; k < kGroup; k++) {
+            const int t = gi * kGroup + k;  // < kTileT: the padding slots carry zeros
+            tu[k] = tgt[t];
+            tv[k] = tgt[kTileT + t];
+            tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : 0.0;
+            tg[k] = tgt[DIM * kTileT + t];
+            tm[k] = tmk[t];
+            a[k] = 0.0;
+          }
+#pragma unroll
+          for (int m = 0; m < kSymM; m++)
+#pragma unroll
+            for (int k = 0; k < kGroup; k++) {
+              const double du = tu[k] - px[m], dv = tv[k] - py[m];
+              double d2 = du * du;
+              d2 = fma(dv, dv, d2);
+              if (DIM == 3) {
+                const double dw = tw[k] - pz[m];
+                d2 = fma(dw, dw, d2);
+              }
+              const double magic = 6755399441055744.0;  // 1.5 * 2^52 (see k_gauss)
+              const double kd = fma(d2, kexp, magic);
+              const int kk = __double2loint(kd);
+              const double r = fma(-d2, kexp, kd - magic);
+              const int j8 = kk & (ET::n - 1);
+              const int m20 = min(kk >> ET::bits, 900) << 20;
+              double q;
+              if constexpr (ET::poly == 4) {
+                const double2 c01 = *(const double2*)(tab + 4 * j8);
+                const double2 c23 = *(const double2*)(tab + 4 * j8 + 2);
+                q = hi_sub(c23.y, m20);
+                q = fma(r, q, hi_sub(c23.x, m20));
+                q = fma(r, q, hi_sub(c01.y, m20));
+                q = fma(r, q, hi_sub(c01.x, m20));
+              } else {
+                const double* cjt = tab + ET::poly * j8;
+                q = hi_sub(cjt[ET::poly - 1], m20);
+#pragma unroll
+                for (int i = ET::poly - 2; i >= 0; i--) q = fma(r, q, hi_sub(cjt[i], m20));
+              }
+              a[k] = fma(pg[m], q, a[k]);  // row i (pg = 0 unless j is in T(c1))
+              // row j: target i in T(c(j)), its bits at c(j)'s offset
+              unsigned long long bit = (tm[k] >> kx[m]) & (tm[k] >> ky[m]);
+              if (DIM == 3) bit &= tm[k] >> kz[m];
+              const double gi_w = (!self[m] && (bit & 1ull)) ? tg[k] : 0.0;
+              accs[m] = fma(gi_w, q, accs[m]);
+            }
+#pragma unroll
+          for (int k = 0; k < kGroup; k++) {
+            const double s = warp_sum(a[k]);
+            const int t = gi * kGroup + k;
+            if (lane == 0 && t < nt) acct[wid * kTileT + t] += s;
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < kSymM; m++) {
+          const int idx = s0 + lane + m * kWarps * 32;
+          if (valid[m] && !self[m]) {
+            const int ddx = kx[m] - nb, ddy = ky[m] - kMaskY - nb, ddz = DIM == 3 ? kz[m] - kMaskZ - nb : 0;
+            const int key = (ddz * W + ddx) * W + ddy;  // > 0 for the upper half of the window
+            part[(long long)(key - 1) * pstride + cj[idx]] = accs[m] * kc.norm;
+          }
+        }
+      }
+      ncomp = 0;
+    };
+
+    while (true) {
+      // ---- plan and issue one fill (thread 0) -----------------------------------------
+      if (tid == 0) {
+        int r = s_cursor[0], p = s_cursor[1];
+        int used = 0, np = 0, valid = 0;
+        unsigned bytes = 0;
+        while (r < nranges && np < kMaxPieces && RC - used >= 4) {
+          int a, b, ddx, ddz;
+          sym_range(g, cs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a, b, ddx, ddz);
+          int s = p < 0 ? a : p;
+          if (s >= b) {
+            r++;
+            p = -1;
+            continue;
+          }
+          int s_al = s & ~1;
+          int room = (RC - used) & ~1;
+          int e_al = min((b + 1) & ~1, s_al + room);
+          int e = min(b, e_al);
+          pieces[np].raw_off = used + (s - s_al);
+          pieces[np].count = e - s;
+          pieces[np].gstart = s;
+          prange[np] = r;
+          np++;
+          valid += e - s;
+          used += e_al - s_al;
+          bytes += (unsigned)(e_al - s_al) * 8u * NA;
+          if (e >= b) {
+            r++;
+            p = -1;
+          } else {
+            p = e;
+          }
+        }
+        s_cursor[0] = r;
+        s_cursor[1] = p;
+        s_fill[0] = np;
+        s_fill[1] = valid;
+        s_fill[2] = (np == 0);
+        if (np > 0) {
+          fence_proxy_async_smem();
+          mbar_expect_tx(bar, bytes);
+          for (int q = 0; q < np; q++) {
+            int s = pieces[q].gstart, s_al = s & ~1;
+            int len = ((s + pieces[q].count + 1) & ~1) - s_al;
+            int dst = pieces[q].raw_off - (s - s_al);
+            bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
+            bulk_g2s(raw + RC + dst, sy + s_al, len * 8u, bar);
+            if (DIM == 3) bulk_g2s(raw + 2 * RC + dst, sz + s_al, len * 8u, bar);
+            bulk_g2s(raw + DIM * RC + dst, sg + s_al, len * 8u, bar);
+            bulk_g2s(raw + (DIM + 1) * RC + dst, pcy + s_al, len * 8u, bar);
+          }
+        }
+      }
+      __syncthreads();
+      if (s_fill[2]) break;
+      if (!mbar_wait(bar, phase)) {
+        if (tid == 0) {
+          atomicOr(err, DEV_ERR_TIMEOUT);
+          s_abort = 1;
+        }
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (s_abort) {
+        mbar_wait(bar, phase ^ 1u, 1u << 20);
+        return;
+      }
+      if (ncomp + s_fill[1] > KC) {
+        flush();
+        __syncthreads();
+      }
+      const int np = s_fill[0];
+      for (int q = 0; q < np; q++) {
+        const Piece pc = pieces[q];
+        const int r = prange[q];
+        int a_, b_, ddx, ddz;
+        sym_range(g, cs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a_, b_, ddx, ddz);
+        for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
+          const int e = e0 + tid;
+          bool in = false;
+          double vx = 0, vy = 0, vz = 0, vg = 0;
+          int code = -1, j = 0;
+          if (e < pc.count) {
+            j = pc.gstart + e;
+            const int ro = pc.raw_off + e;
+            vx = raw[ro];
+            vy = raw[RC + ro];
+            if (DIM == 3) vz = raw[2 * RC + ro];
+            vg = raw[DIM * RC + ro];
+            if (r == 0) {
+              in = true;  // the centre cell, unconditionally (2d/get_trunc.h:31-39)
+            } else {
+              const int ddy = (int)__double_as_longlong(raw[(DIM + 1) * RC + ro]) - iy;
+              // j in T(c1): the box test against c1's centre (2d/get_trunc.h:63)
+              bool fij = fabs(vx - xc) < L && fabs(vy - yc) < L;
+              if (DIM == 3) fij = fij && fabs(vz - zc) < L;
+              // some target of c1 may lie in T(c(j)): keep the source for row j
+              unsigned long long pb = (tor >> (ddx + nb)) & (tor >> (kMaskY + ddy + nb));
+              if (DIM == 3) pb &= tor >> (kMaskZ + ddz + nb);
+              in = fij || (pb & 1ull);
+              if (!fij) vg = 0.0;
+              code = (ddx + nb) | ((ddy + nb) << 8) | ((ddz + nb) << 16);
+            }
+          }
+          unsigned bal = __ballot_sync(0xffffffffu, in);
+          if (lane == 0) s_wsum[wid] = __popc(bal);
+          __syncthreads();
+          int pre = 0, tot = 0;
+#pragma unroll
+          for (int k = 0; k < kWarps; k++) {
+            const int c = s_wsum[k];
+            pre += k < wid ? c : 0;
+            tot += c;
+          }
+          if (in) {
+            const int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
+            comp[pos] = vx - xc;
+            comp[KC + pos] = vy - yc;
+            if (DIM == 3) comp[2 * KC + pos] = vz - zc;
+            comp[DIM * KC + pos] = vg;
+            ccode[pos] = code;
+            cj[pos] = j;
+          }
+          ncomp += tot;
+          __syncthreads();
+        }
+      }
+    }
+    flush();
+    __syncthreads();
+    for (int t = tid; t < nt; t += kThreads) {
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < kWarps; q++) s += acct[q * kTileT + t];
+      w[t0 + t] = s * kc.norm;
+    }
+  }
+}
+
+// Rows += their partial slots (offset order), slots back to zero for the next product.
+__global__ void k_sym_gather(int n, int K, long long pstride, double* __restrict__ part, double* __restrict__ w,
+                             const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int o = 0; o < K; o++) {
+      const double v = part[(long long)o * pstride + i];
+      if (v != 0.0) {
+        s += v;
+        part[(long long)o * pstride + i] = 0.0;
+      }
+    }
+    w[i] += s;
+  }
+}
+
+// Cell y index of every sorted point (the symmetric sum's per-source cell), as 64-bit words.
+__global__ void k_cell_y(Grid g, const int* __restrict__ cs, unsigned long long* __restrict__ out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    cell_xyz(g, c, ix, iy, iz);
+    for (int j = cs[c]; j < cs[c + 1]; j++) out[j] = (unsigned long long)iy;
+  }
+}
+
+__global__ void k_max_cell(int ncell, const int* __restrict__ cs, int* __restrict__ out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncell) atomicMax(out, cs[c + 1] - cs[c]);
+}
+
 // ---- work list and truncation-set sizes ----------------------------------------------
 __global__ void k_item_counts(int ncell, const int* __restrict__ cs_t, int* __restrict__ cnt) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -864,6 +1293,28 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   PRBF_CHECK_LAUNCH();
 }
 
+template <int DIM>
+void launch_sym(const GaussPlan& P, const PointsView& s, const double* gv, double* w, unsigned* err, const int* skip,
+                cudaStream_t st) {
+  constexpr size_t sm = LayoutS<DIM>::total;
+  static_assert(sm <= 227 * 1024, "k_gauss_sym shared memory");
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  PRBF_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !attr_set[dev]) {
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_sym<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (dev < 64) attr_set[dev] = true;
+  }
+  const SumConsts k0 = sum_consts(P.g.sigma, false, LayoutS<DIM>::ET::n);
+  const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
+  k_gauss_sym<DIM><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, s.x, s.y, s.z, gv, P.sym_cy.get(),
+                                               s.cell_start, w, P.sym_part.get(), P.sym_pstride, k0, err, skip);
+  PRBF_CHECK_LAUNCH();
+  const int gb = std::max(1, std::min(ceil_div(s.n, 256), 8 * 152));
+  k_sym_gather<<<gb, 256, 0, st>>>(s.n, P.sym_K, P.sym_pstride, P.sym_part.get(), w, skip);
+  PRBF_CHECK_LAUNCH();
+}
+
 template <int DIM, int NV, bool BATCH>
 void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, const double* gv, double* w,
                  long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
@@ -945,7 +1396,7 @@ static void alloc_f32(GaussPlan& plan, int dim, int n, cudaStream_t s) {
 }
 
 void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& src, unsigned* err,
-                    Workspace& ws, cudaStream_t s) {
+                    Workspace& ws, cudaStream_t s, bool forms) {
   (void)err;
   const Grid& g = plan.g;
   int* cnt = (int*)ws.get(20, sizeof(int) * ((size_t)g.ncell + 1));
@@ -980,6 +1431,8 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
   upload_table(s);
   // FP32 form's source data
   plan.f32_ready = false;
+  plan.sym_ready = false;
+  if (!forms) return;
   if (f32_grid_ok(g) && src.n > 0) {
     alloc_f32(plan, g.dim, src.n, s);
     const SumConsts k32 = sum_consts(g.sigma, true, 0);
@@ -987,6 +1440,36 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
                                                      plan.su.get(), plan.sv.get(), plan.sw.get(), plan.smask.get());
     PRBF_CHECK_LAUNCH();
     plan.f32_ready = true;
+  }
+  // symmetric FP64 matvec: the same point set on both sides, every cell within one item
+  // (<= kTileT points), 2 nb + 1 mask bits per axis, and the partial slots within 1/8 of
+  // the free device memory
+  if (tgt.x == src.x && tgt.n == src.n && src.n > 0 && 2 * g.nb_trunc + 1 <= kMaskBits && (g.dim == 2 || g.dim == 3)) {
+    int* dmax = (int*)ws.get(25, sizeof(int));
+    PRBF_CUDA(cudaMemsetAsync(dmax, 0, sizeof(int), s));
+    k_max_cell<<<ceil_div(g.ncell, 256), 256, 0, s>>>(g.ncell, src.cell_start, dmax);
+    PRBF_CHECK_LAUNCH();
+    int hmax = 0;
+    PRBF_CUDA(cudaMemcpyAsync(&hmax, dmax, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PRBF_CUDA(cudaStreamSynchronize(s));
+    const int W = 2 * g.nb_trunc + 1;
+    const int K = g.dim == 2 ? (W * W - 1) / 2 : (W * W * W - 1) / 2;
+    const long long pstride = ((long long)src.n + 8 + 31) / 32 * 32;
+    size_t free_b = 0, total_b = 0;
+    PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const double bytes = (double)K * pstride * sizeof(double) + (double)(src.n + 8) * 8;
+    if (hmax <= kTileT && K >= 1 && bytes <= 0.125 * (double)free_b) {
+      plan.sym_K = K;
+      plan.sym_pstride = pstride;
+      plan.sym_part.reserve((size_t)K * pstride);
+      PRBF_CUDA(cudaMemsetAsync(plan.sym_part.get(), 0, sizeof(double) * (size_t)K * pstride, s));
+      plan.sym_cy.reserve((size_t)src.n + 8);
+      PRBF_CUDA(cudaMemsetAsync(plan.sym_cy.get(), 0, sizeof(unsigned long long) * ((size_t)src.n + 8), s));
+      k_cell_y<<<std::max(1, std::min(ceil_div(g.ncell, 256), 8 * 152)), 256, 0, s>>>(g, src.cell_start,
+                                                                                   plan.sym_cy.get());
+      PRBF_CHECK_LAUNCH();
+      plan.sym_ready = true;
+    }
   }
 }
 
@@ -1013,6 +1496,13 @@ void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s,
   if (P.nitems == 0 || nv <= 0) return;
   if (nv > 1 && (vstride % 2 || vstride < t.n || vstride < s.n))
     throw Error(PRBF_ERR_ARG, "vector stride must be even and cover the points");
+  if (!fp32 && nv == 1 && P.sym_ready && !P.batched && t.x == s.x && t.n == s.n) {
+    if (P.g.dim == 2)
+      launch_sym<2>(P, s, gv, w, err, skip, st);
+    else
+      launch_sym<3>(P, s, gv, w, err, skip, st);
+    return;
+  }
   if (P.g.dim == 2) {
     if (fp32)
       launch_nv<2, true>(P, t, s, gv, w, nv, vstride, err, skip, st);
