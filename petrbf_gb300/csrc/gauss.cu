@@ -742,12 +742,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
 // written by one CTA only -- and k_sym_gather adds the slots to the rows in a fixed order,
 // zeroing them for the next product. Two ordered pairs cost 12 FP64 instructions in 2D
 // (distance 4, exponential 6, two accumulations) against 2 x 11.
-// Lanes own sources (kSymM at a time), each warp walks all targets in groups of kGroup, and
+// Lanes own sources (SPL at a time), each warp walks all targets in groups of kGroup, and
 // the per-target sums go to per-warp rows of shared memory that are added in warp order
 // at the end: the result does not depend on scheduling.
 constexpr int kSymRC = 512;   // staged sources per fill
 constexpr int kSymKC = 1024;  // compacted sources
-constexpr int kSymM = 2;      // sources per lane at a time
 
 template <int DIM>
 struct LayoutS {
@@ -817,6 +816,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
   using Lay = LayoutS<DIM>;
   using ET = typename Lay::ET;
   constexpr int NA = Lay::NA, RC = kSymRC, KC = kSymKC;
+  // sources per lane at a time: each group of kGroup targets ends in kGroup warp
+  // reductions (5 FP64 adds per lane each), amortised over SPL x kGroup pairs
+  constexpr int SPL = 4;
   extern __shared__ __align__(16) unsigned char smem[];
   double* raw = (double*)(smem + Lay::raw);
   double* comp = (double*)(smem + Lay::comp);
@@ -897,12 +899,12 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     int ncomp = 0;
     const int ngroups = (nt + kGroup - 1) / kGroup;
     auto flush = [&]() {
-      for (int s0 = wid * 32; s0 < ncomp; s0 += kWarps * 32 * kSymM) {
-        double px[kSymM], py[kSymM], pz[kSymM], pg[kSymM], accs[kSymM];
-        int kx[kSymM], ky[kSymM], kz[kSymM];
-        bool self[kSymM], valid[kSymM];
+      for (int s0 = wid * 32; s0 < ncomp; s0 += kWarps * 32 * SPL) {
+        double px[SPL], py[SPL], pz[SPL], pg[SPL], accs[SPL];
+        int kx[SPL], ky[SPL], kz[SPL];
+        bool self[SPL], valid[SPL];
 #pragma unroll
-        for (int m = 0; m < kSymM; m++) {
+        for (int m = 0; m < SPL; m++) {
           const int idx = s0 + lane + m * kWarps * 32;
           valid[m] = idx < ncomp;
           const int cd = valid[m] ? ccode[idx] : -1;
@@ -930,7 +932,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             a[k] = 0.0;
           }
 #pragma unroll
-          for (int m = 0; m < kSymM; m++)
+          for (int m = 0; m < SPL; m++)
 #pragma unroll
             for (int k = 0; k < kGroup; k++) {
               const double du = tu[k] - px[m], dv = tv[k] - py[m];
@@ -967,15 +969,23 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
               const double gi_w = (!self[m] && (bit & 1ull)) ? tg[k] : 0.0;
               accs[m] = fma(gi_w, q, accs[m]);
             }
-#pragma unroll
-          for (int k = 0; k < kGroup; k++) {
-            const double s = warp_sum(a[k]);
-            const int t = gi * kGroup + k;
-            if (lane == 0 && t < nt) acct[wid * kTileT + t] += s;
-          }
+          // the four target sums over the warp by a butterfly that halves the values each
+          // lane carries (6 FP64 adds per lane instead of 4 x 5): lane 8 k ends with target k
+          static_assert(kGroup == 4, "reduce-scatter of four sums");
+          const bool h16 = lane & 16, h8 = lane & 8;
+          double k0 = h16 ? a[2] : a[0], k1 = h16 ? a[3] : a[1];
+          k0 += __shfl_xor_sync(0xffffffffu, h16 ? a[0] : a[2], 16);
+          k1 += __shfl_xor_sync(0xffffffffu, h16 ? a[1] : a[3], 16);
+          double kp = h8 ? k1 : k0;
+          kp += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 4);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 2);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 1);
+          const int t = gi * kGroup + (lane >> 3);
+          if ((lane & 7) == 0 && t < nt) acct[wid * kTileT + t] += kp;
         }
 #pragma unroll
-        for (int m = 0; m < kSymM; m++) {
+        for (int m = 0; m < SPL; m++) {
           const int idx = s0 + lane + m * kWarps * 32;
           if (valid[m] && !self[m]) {
             const int ddx = kx[m] - nb, ddy = ky[m] - kMaskY - nb, ddz = DIM == 3 ? kz[m] - kMaskZ - nb : 0;
