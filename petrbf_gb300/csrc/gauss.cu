@@ -901,7 +901,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     auto flush = [&]() {
       for (int s0 = wid * 32; s0 < ncomp; s0 += kWarps * 32 * SPL) {
         double px[SPL], py[SPL], pz[SPL], pg[SPL], accs[SPL];
-        int kx[SPL], ky[SPL], kz[SPL];
+        int kx[SPL], ky[SPL], kz[SPL], sidx[SPL], smax[SPL];
         bool self[SPL], valid[SPL];
 #pragma unroll
         for (int m = 0; m < SPL; m++) {
@@ -909,6 +909,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
           valid[m] = idx < ncomp;
           const int cd = valid[m] ? ccode[idx] : -1;
           self[m] = cd < 0;
+          // c1's own points are compacted first, in order: source position idx is target
+          // idx. Their pairs are taken once (idx >= t), both rows inside c1; a warp whose
+          // own points all precede a group's targets skips that group.
+          sidx[m] = idx;
+          smax[m] = __reduce_max_sync(0xffffffffu, !valid[m] ? -1 : (self[m] ? idx : 0x7fffffff));
           kx[m] = cd & 255;
           ky[m] = kMaskY + ((cd >> 8) & 255);
           kz[m] = kMaskZ + ((cd >> 16) & 255);
@@ -932,9 +937,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             a[k] = 0.0;
           }
 #pragma unroll
-          for (int m = 0; m < SPL; m++)
+          for (int m = 0; m < SPL; m++) {
+            if (smax[m] < gi * kGroup) continue;
 #pragma unroll
             for (int k = 0; k < kGroup; k++) {
+              const int t = gi * kGroup + k;
               const double du = tu[k] - px[m], dv = tv[k] - py[m];
               double d2 = du * du;
               d2 = fma(dv, dv, d2);
@@ -962,13 +969,17 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
 #pragma unroll
                 for (int i = ET::poly - 2; i >= 0; i--) q = fma(r, q, hi_sub(cjt[i], m20));
               }
-              a[k] = fma(pg[m], q, a[k]);  // row i (pg = 0 unless j is in T(c1))
-              // row j: target i in T(c(j)), its bits at c(j)'s offset
+              // row i (pg = 0 unless j is in T(c1)); own points: the pair once, idx >= t
+              const bool use_i = !self[m] || sidx[m] >= t;
+              a[k] = fma(use_i ? pg[m] : 0.0, q, a[k]);
+              // row j: target i in T(c(j)) -- its bits at c(j)'s offset -- or, for an own
+              // point, the other row of the pair (idx > t)
               unsigned long long bit = (tm[k] >> kx[m]) & (tm[k] >> ky[m]);
               if (DIM == 3) bit &= tm[k] >> kz[m];
-              const double gi_w = (!self[m] && (bit & 1ull)) ? tg[k] : 0.0;
-              accs[m] = fma(gi_w, q, accs[m]);
+              const bool use_j = self[m] ? sidx[m] > t : (bit & 1ull) != 0;
+              accs[m] = fma(use_j ? tg[k] : 0.0, q, accs[m]);
             }
+          }
           // the four target sums over the warp by a butterfly that halves the values each
           // lane carries (6 FP64 adds per lane instead of 4 x 5): lane 8 k ends with target k
           static_assert(kGroup == 4, "reduce-scatter of four sums");
@@ -984,15 +995,18 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
           const int t = gi * kGroup + (lane >> 3);
           if ((lane & 7) == 0 && t < nt) acct[wid * kTileT + t] += kp;
         }
+        __syncwarp();  // the group sums' writes to this warp's row come first
 #pragma unroll
         for (int m = 0; m < SPL; m++) {
           const int idx = s0 + lane + m * kWarps * 32;
+          if (valid[m] && self[m]) acct[wid * kTileT + idx] += accs[m];  // row idx of c1 itself
           if (valid[m] && !self[m]) {
             const int ddx = kx[m] - nb, ddy = ky[m] - kMaskY - nb, ddz = DIM == 3 ? kz[m] - kMaskZ - nb : 0;
             const int key = (ddz * W + ddx) * W + ddy;  // > 0 for the upper half of the window
             part[(long long)(key - 1) * pstride + cj[idx]] = accs[m] * kc.norm;
           }
         }
+        __syncwarp();
       }
       ncomp = 0;
     };
