@@ -146,6 +146,11 @@ int prbf_matvec_dev(prbf_ctx* ctx, const double* x_in_dev, double* y_out_dev, in
  * start offsets (ncell+1 ints), truncation-set sizes (ncell ints), and grid info
  * (ints: nx ny nz ncell nb_trunc nb_buffer max_trunc; doubles: xmin ymin zmin box). */
 int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs);
+/* Kernels one cell-order product of the matvec seam launches (fp32 = 0: the FP64 sum, 2
+ * when it takes the symmetric form -- each exponential used for both rows of a point pair,
+ * the reverse contributions added by a second kernel -- else 1; fp32 = 1: the weight
+ * conversion and the FP32 sum) and whether the FP64 product is symmetric. */
+int prbf_matvec_kernels(prbf_ctx* ctx, int fp32, int* kernels, int* symmetric);
 int prbf_get_permutation(prbf_ctx* ctx, int* perm_out);
 int prbf_get_cell_start(prbf_ctx* ctx, int* cell_start_out);
 int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);

@@ -82,6 +82,8 @@ SIGNATURES = {
     "prbf_matvec_setup": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _D, _D, _D]),
     "prbf_matvec": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
     "prbf_matvec_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "prbf_matvec_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int)]),
     "prbf_matvec_info": (ctypes.c_int, [ctypes.c_void_p, _I, _D, ctypes.POINTER(ctypes.c_longlong)]),
     "prbf_get_permutation": (ctypes.c_int, [ctypes.c_void_p, _I]),
     "prbf_get_cell_start": (ctypes.c_int, [ctypes.c_void_p, _I]),

@@ -91,6 +91,12 @@ class Context:
         self._check(N.lib().prbf_matvec_dev(self.h, ctypes.c_void_p(in_ptr),
                                              ctypes.c_void_p(out_ptr), flags))
 
+    def matvec_kernels(self, fp32=False):
+        """(kernels one cell-order product launches, whether the FP64 product is symmetric)."""
+        k, sym = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(N.lib().prbf_matvec_kernels(self.h, 1 if fp32 else 0, ctypes.byref(k), ctypes.byref(sym)))
+        return k.value, bool(sym.value)
+
     def matvec_info(self):
         ints = np.zeros(7, np.int32)
         dbls = np.zeros(4, np.float64)

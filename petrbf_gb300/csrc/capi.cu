@@ -293,6 +293,15 @@ int prbf_matvec(prbf_ctx* ctx, const double* xin, double* yout) {
   });
 }
 
+int prbf_matvec_kernels(prbf_ctx* ctx, int fp32, int* kernels, int* symmetric) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
+    const bool sym = !fp32 && c.mv_plan.sym_ready;
+    if (kernels) *kernels = fp32 ? (c.mv_plan.f32_ready ? 2 : 1) : (sym ? 2 : 1);
+    if (symmetric) *symmetric = sym ? 1 : 0;
+  });
+}
+
 int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs) {
   return guarded(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
