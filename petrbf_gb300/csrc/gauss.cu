@@ -1159,7 +1159,7 @@ __global__ void k_sym_gather(int n, int K, long long pstride, double* __restrict
     double s = 0.0;
     for (int o = 0; o < K; o++) {
       const double v = part[(long long)o * pstride + i];
-      if (v != 0.0) {
+      if (__double_as_longlong(v) != 0) {  // an integer test: the FP64 pipe is for the sums
         s += v;
         part[(long long)o * pstride + i] = 0.0;
       }
