@@ -101,9 +101,11 @@ struct GaussPlan {
   DevBuf<float> su, sv, sw, g32;
   DevBuf<unsigned long long> smask;
   // FP64 matvec with each exponential used for both rows (targets == sources, every cell
-  // <= 128 points): K partial slots of pstride entries (kept zero between products) and
+  // <= 128 points): K partial slots of pstride entries per weight vector, for up to sym_nv
+  // vectors per launch (set sym_nv before gauss_plan_dev; kept zero between products), and
   // each point's cell y index
   bool sym_ready = false;
+  int sym_nv = 1;
   int sym_K = 0;
   long long sym_pstride = 0;
   DevBuf<double> sym_part;

@@ -746,20 +746,22 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
 // the per-target sums go to per-warp rows of shared memory that are added in warp order
 // at the end: the result does not depend on scheduling.
 constexpr int kSymRC = 512;   // staged sources per fill
-constexpr int kSymKC = 1024;  // compacted sources
+constexpr int kSymMaxK = 32;  // partial slots per point and vector (upper window cells)
 
-template <int DIM>
+// NV weight vectors (right-hand sides) share each pair's exponential, as in k_gauss.
+template <int DIM, int NV>
 struct LayoutS {
-  static constexpr int NA = DIM + 2;  // staged arrays: coordinates, weight, cell-y word
-  using ET = ExpTab<DIM == 2>;        // 2D: the 1024-entry table (one weight vector)
+  static constexpr int KC = NV == 1 ? 1024 : 768;  // compacted sources
+  static constexpr int NA = DIM + NV + 1;  // staged arrays: coordinates, weights, cell-y word
+  using ET = ExpTab<UseBigTab<DIM, NV>::v>;
   static constexpr size_t raw = 0;                                                     // NA x RC
-  static constexpr size_t comp = align16(raw + sizeof(double) * NA * kSymRC);           // (DIM+1) x KC
-  static constexpr size_t code = align16(comp + sizeof(double) * (DIM + 1) * kSymKC);   // KC
-  static constexpr size_t jidx = align16(code + sizeof(int) * kSymKC);                  // KC
-  static constexpr size_t tgt = align16(jidx + sizeof(int) * kSymKC);                   // (DIM+1) x kTileT
-  static constexpr size_t tmask = align16(tgt + sizeof(double) * (DIM + 1) * kTileT);   // kTileT
-  static constexpr size_t acct = align16(tmask + sizeof(unsigned long long) * kTileT);  // kWarps x kTileT
-  static constexpr size_t tab = align16(acct + sizeof(double) * kWarps * kTileT);
+  static constexpr size_t comp = align16(raw + sizeof(double) * NA * kSymRC);           // (DIM+NV) x KC
+  static constexpr size_t code = align16(comp + sizeof(double) * (DIM + NV) * KC);      // KC
+  static constexpr size_t jidx = align16(code + sizeof(int) * KC);                      // KC
+  static constexpr size_t tgt = align16(jidx + sizeof(int) * KC);                       // (DIM+NV) x kTileT
+  static constexpr size_t tmask = align16(tgt + sizeof(double) * (DIM + NV) * kTileT);  // kTileT
+  static constexpr size_t acct = align16(tmask + sizeof(unsigned long long) * kTileT);  // kWarps x NV x kTileT
+  static constexpr size_t tab = align16(acct + sizeof(double) * kWarps * NV * kTileT);
   static constexpr size_t pieces = align16(tab + sizeof(double) * ET::poly * ET::n);
   static constexpr size_t prange = align16(pieces + sizeof(Piece) * kMaxPieces);
   static constexpr size_t bar = align16(prange + sizeof(int) * kMaxPieces);
@@ -806,19 +808,19 @@ __device__ __forceinline__ void sym_range(const Grid& g, const int* __restrict__
   b = cs[cb + cell_of(g, cx, jy1, cz) + 1];
 }
 
-template <int DIM>
+template <int DIM, int NV>
 __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     Grid g, const int2* __restrict__ items, int nitems, const double* __restrict__ sx,
-    const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg,
+    const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg, long long vs,
     const unsigned long long* __restrict__ pcy, const int* __restrict__ cs, double* __restrict__ w,
-    double* __restrict__ part, long long pstride, SumConsts kc, unsigned* err, const int* __restrict__ skip) {
+    double* __restrict__ part, long long pstride, int K, SumConsts kc, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  using Lay = LayoutS<DIM>;
+  using Lay = LayoutS<DIM, NV>;
   using ET = typename Lay::ET;
-  constexpr int NA = Lay::NA, RC = kSymRC, KC = kSymKC;
-  // sources per lane at a time: each group of kGroup targets ends in kGroup warp
-  // reductions (5 FP64 adds per lane each), amortised over SPL x kGroup pairs
-  constexpr int SPL = 4;
+  constexpr int NA = Lay::NA, RC = kSymRC, KC = Lay::KC;
+  // sources per lane at a time: each group of kGroup targets ends in a warp reduction of
+  // its kGroup x NV sums, amortised over SPL x kGroup pairs
+  constexpr int SPL = NV == 1 ? 4 : 2;
   extern __shared__ __align__(16) unsigned char smem[];
   double* raw = (double*)(smem + Lay::raw);
   double* comp = (double*)(smem + Lay::comp);
@@ -838,7 +840,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
   __shared__ unsigned long long s_tor;
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (DIM == 2 ? d_tab_big : d_tab_small)[i];
+  for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (UseBigTab<DIM, NV>::v ? d_tab_big : d_tab_small)[i];
   if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
   const int G = gridDim.x;
@@ -864,13 +866,16 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     if (tid == 0) s_tor = 0ull;
     __syncthreads();
     for (int t = tid; t < kTileT; t += kThreads) {
-      double xt = 0.0, yt = 0.0, zt = 0.0, gt = 0.0;
+      double xt = 0.0, yt = 0.0, zt = 0.0, gt[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) gt[v] = 0.0;
       unsigned long long m = 0ull;
       if (t < nt) {
         xt = sx[t0 + t];
         yt = sy[t0 + t];
         if (DIM == 3) zt = sz[t0 + t];
-        gt = sg[t0 + t];
+#pragma unroll
+        for (int v = 0; v < NV; v++) gt[v] = sg[v * vs + t0 + t];
         // the reference's box test of this point against the centres of the cells at
         // offsets -nb .. nb of its own (2d/get_trunc.h:63): bit o + nb per axis
         for (int o = -nb; o <= nb; o++) {
@@ -883,10 +888,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
       tgt[t] = xt - xc;
       tgt[kTileT + t] = yt - yc;
       if (DIM == 3) tgt[2 * kTileT + t] = zt - zc;
-      tgt[DIM * kTileT + t] = gt;  // zero for the padding slots: they add nothing to a row j
+#pragma unroll
+      for (int v = 0; v < NV; v++) tgt[(DIM + v) * kTileT + t] = gt[v];  // zero in the padding slots
       tmk[t] = m;
 #pragma unroll
-      for (int q = 0; q < kWarps; q++) acct[q * kTileT + t] = 0.0;
+      for (int q = 0; q < kWarps * NV; q++) acct[q * kTileT + t] = 0.0;
     }
     if (tid == 0) {
       s_cursor[0] = 0;
@@ -900,7 +906,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     const int ngroups = (nt + kGroup - 1) / kGroup;
     auto flush = [&]() {
       for (int s0 = wid * 32; s0 < ncomp; s0 += kWarps * 32 * SPL) {
-        double px[SPL], py[SPL], pz[SPL], pg[SPL], accs[SPL];
+        double px[SPL], py[SPL], pz[SPL], pg[SPL][NV], accs[SPL][NV];
         int kx[SPL], ky[SPL], kz[SPL], sidx[SPL], smax[SPL];
         bool self[SPL], valid[SPL];
 #pragma unroll
@@ -920,11 +926,14 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
           px[m] = valid[m] ? comp[idx] : 0.0;
           py[m] = valid[m] ? comp[KC + idx] : 0.0;
           pz[m] = (DIM == 3 && valid[m]) ? comp[2 * KC + idx] : 0.0;
-          pg[m] = valid[m] ? comp[DIM * KC + idx] : 0.0;
-          accs[m] = 0.0;
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            pg[m][v] = valid[m] ? comp[(DIM + v) * KC + idx] : 0.0;
+            accs[m][v] = 0.0;
+          }
         }
         for (int gi = 0; gi < ngroups; gi++) {
-          double tu[kGroup], tv[kGroup], tw[kGroup], tg[kGroup], a[kGroup];
+          double tu[kGroup], tv[kGroup], tw[kGroup], tg[kGroup][NV], a[kGroup][NV];
           unsigned long long tm[kGroup];
 #pragma unroll
           for (int k = 0; k < kGroup; k++) {
@@ -932,9 +941,12 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             tu[k] = tgt[t];
             tv[k] = tgt[kTileT + t];
             tw[k] = DIM == 3 ? tgt[2 * kTileT + t] : 0.0;
-            tg[k] = tgt[DIM * kTileT + t];
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+              tg[k][v] = tgt[(DIM + v) * kTileT + t];
+              a[k][v] = 0.0;
+            }
             tm[k] = tmk[t];
-            a[k] = 0.0;
           }
 #pragma unroll
           for (int m = 0; m < SPL; m++) {
@@ -971,39 +983,48 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
               }
               // row i (pg = 0 unless j is in T(c1)); own points: the pair once, idx >= t
               const bool use_i = !self[m] || sidx[m] >= t;
-              a[k] = fma(use_i ? pg[m] : 0.0, q, a[k]);
+#pragma unroll
+              for (int v = 0; v < NV; v++) a[k][v] = fma(use_i ? pg[m][v] : 0.0, q, a[k][v]);
               // row j: target i in T(c(j)) -- its bits at c(j)'s offset -- or, for an own
               // point, the other row of the pair (idx > t)
               unsigned long long bit = (tm[k] >> kx[m]) & (tm[k] >> ky[m]);
               if (DIM == 3) bit &= tm[k] >> kz[m];
               const bool use_j = self[m] ? sidx[m] > t : (bit & 1ull) != 0;
-              accs[m] = fma(use_j ? tg[k] : 0.0, q, accs[m]);
+#pragma unroll
+              for (int v = 0; v < NV; v++) accs[m][v] = fma(use_j ? tg[k][v] : 0.0, q, accs[m][v]);
             }
           }
           // the four target sums over the warp by a butterfly that halves the values each
           // lane carries (6 FP64 adds per lane instead of 4 x 5): lane 8 k ends with target k
           static_assert(kGroup == 4, "reduce-scatter of four sums");
           const bool h16 = lane & 16, h8 = lane & 8;
-          double k0 = h16 ? a[2] : a[0], k1 = h16 ? a[3] : a[1];
-          k0 += __shfl_xor_sync(0xffffffffu, h16 ? a[0] : a[2], 16);
-          k1 += __shfl_xor_sync(0xffffffffu, h16 ? a[1] : a[3], 16);
-          double kp = h8 ? k1 : k0;
-          kp += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
-          kp += __shfl_xor_sync(0xffffffffu, kp, 4);
-          kp += __shfl_xor_sync(0xffffffffu, kp, 2);
-          kp += __shfl_xor_sync(0xffffffffu, kp, 1);
           const int t = gi * kGroup + (lane >> 3);
-          if ((lane & 7) == 0 && t < nt) acct[wid * kTileT + t] += kp;
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            double k0 = h16 ? a[2][v] : a[0][v], k1 = h16 ? a[3][v] : a[1][v];
+            k0 += __shfl_xor_sync(0xffffffffu, h16 ? a[0][v] : a[2][v], 16);
+            k1 += __shfl_xor_sync(0xffffffffu, h16 ? a[1][v] : a[3][v], 16);
+            double kp = h8 ? k1 : k0;
+            kp += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
+            kp += __shfl_xor_sync(0xffffffffu, kp, 4);
+            kp += __shfl_xor_sync(0xffffffffu, kp, 2);
+            kp += __shfl_xor_sync(0xffffffffu, kp, 1);
+            if ((lane & 7) == 0 && t < nt) acct[(wid * NV + v) * kTileT + t] += kp;
+          }
         }
         __syncwarp();  // the group sums' writes to this warp's row come first
 #pragma unroll
         for (int m = 0; m < SPL; m++) {
           const int idx = s0 + lane + m * kWarps * 32;
-          if (valid[m] && self[m]) acct[wid * kTileT + idx] += accs[m];  // row idx of c1 itself
+          if (valid[m] && self[m])  // row idx of c1 itself
+#pragma unroll
+            for (int v = 0; v < NV; v++) acct[(wid * NV + v) * kTileT + idx] += accs[m][v];
           if (valid[m] && !self[m]) {
             const int ddx = kx[m] - nb, ddy = ky[m] - kMaskY - nb, ddz = DIM == 3 ? kz[m] - kMaskZ - nb : 0;
             const int key = (ddz * W + ddx) * W + ddy;  // > 0 for the upper half of the window
-            part[(long long)(key - 1) * pstride + cj[idx]] = accs[m] * kc.norm;
+#pragma unroll
+            for (int v = 0; v < NV; v++)
+              part[((long long)v * K + key - 1) * pstride + cj[idx]] = accs[m][v] * kc.norm;
           }
         }
         __syncwarp();
@@ -1060,8 +1081,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
             bulk_g2s(raw + RC + dst, sy + s_al, len * 8u, bar);
             if (DIM == 3) bulk_g2s(raw + 2 * RC + dst, sz + s_al, len * 8u, bar);
-            bulk_g2s(raw + DIM * RC + dst, sg + s_al, len * 8u, bar);
-            bulk_g2s(raw + (DIM + 1) * RC + dst, pcy + s_al, len * 8u, bar);
+#pragma unroll
+            for (int v = 0; v < NV; v++) bulk_g2s(raw + (DIM + v) * RC + dst, sg + v * vs + s_al, len * 8u, bar);
+            bulk_g2s(raw + (DIM + NV) * RC + dst, pcy + s_al, len * 8u, bar);
           }
         }
       }
@@ -1092,7 +1114,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
         for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
           const int e = e0 + tid;
           bool in = false;
-          double vx = 0, vy = 0, vz = 0, vg = 0;
+          double vx = 0, vy = 0, vz = 0, vg[NV];
+#pragma unroll
+          for (int v = 0; v < NV; v++) vg[v] = 0.0;
           int code = -1, j = 0;
           if (e < pc.count) {
             j = pc.gstart + e;
@@ -1100,11 +1124,12 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             vx = raw[ro];
             vy = raw[RC + ro];
             if (DIM == 3) vz = raw[2 * RC + ro];
-            vg = raw[DIM * RC + ro];
+#pragma unroll
+            for (int v = 0; v < NV; v++) vg[v] = raw[(DIM + v) * RC + ro];
             if (r == 0) {
               in = true;  // the centre cell, unconditionally (2d/get_trunc.h:31-39)
             } else {
-              const int ddy = (int)__double_as_longlong(raw[(DIM + 1) * RC + ro]) - iy;
+              const int ddy = (int)__double_as_longlong(raw[(DIM + NV) * RC + ro]) - iy;
               // j in T(c1): the box test against c1's centre (2d/get_trunc.h:63)
               bool fij = fabs(vx - xc) < L && fabs(vy - yc) < L;
               if (DIM == 3) fij = fij && fabs(vz - zc) < L;
@@ -1112,7 +1137,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
               unsigned long long pb = (tor >> (ddx + nb)) & (tor >> (kMaskY + ddy + nb));
               if (DIM == 3) pb &= tor >> (kMaskZ + ddz + nb);
               in = fij || (pb & 1ull);
-              if (!fij) vg = 0.0;
+              if (!fij)
+#pragma unroll
+                for (int v = 0; v < NV; v++) vg[v] = 0.0;
               code = (ddx + nb) | ((ddy + nb) << 8) | ((ddz + nb) << 16);
             }
           }
@@ -1131,7 +1158,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
             comp[pos] = vx - xc;
             comp[KC + pos] = vy - yc;
             if (DIM == 3) comp[2 * KC + pos] = vz - zc;
-            comp[DIM * KC + pos] = vg;
+#pragma unroll
+            for (int v = 0; v < NV; v++) comp[(DIM + v) * KC + pos] = vg[v];
             ccode[pos] = code;
             cj[pos] = j;
           }
@@ -1142,30 +1170,34 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
     }
     flush();
     __syncthreads();
-    for (int t = tid; t < nt; t += kThreads) {
-      double s = 0.0;
+    for (int t = tid; t < nt; t += kThreads)
 #pragma unroll
-      for (int q = 0; q < kWarps; q++) s += acct[q * kTileT + t];
-      w[t0 + t] = s * kc.norm;
-    }
+      for (int v = 0; v < NV; v++) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kWarps; q++) s += acct[(q * NV + v) * kTileT + t];
+        w[v * vs + t0 + t] = s * kc.norm;
+      }
   }
 }
 
 // Rows += their partial slots (offset order), slots back to zero for the next product.
-__global__ void k_sym_gather(int n, int K, long long pstride, double* __restrict__ part, double* __restrict__ w,
-                             const int* __restrict__ skip) {
+__global__ void k_sym_gather(int n, int nv, int K, long long pstride, double* __restrict__ part,
+                             double* __restrict__ w, long long vs, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int o = 0; o < K; o++) {
-      const double v = part[(long long)o * pstride + i];
-      if (__double_as_longlong(v) != 0) {  // an integer test: the FP64 pipe is for the sums
-        s += v;
-        part[(long long)o * pstride + i] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int v = 0; v < nv; v++) {
+      double s = 0.0;
+      for (int o = 0; o < K; o++) {
+        double* slot = part + ((long long)v * K + o) * pstride + i;
+        const double x = *slot;
+        if (__double_as_longlong(x) != 0) {  // an integer test: the FP64 pipe is for the sums
+          s += x;
+          *slot = 0.0;
+        }
       }
+      w[v * vs + i] += s;
     }
-    w[i] += s;
-  }
 }
 
 // Cell y index of every sorted point (the symmetric sum's per-source cell), as 64-bit words.
@@ -1317,26 +1349,42 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   PRBF_CHECK_LAUNCH();
 }
 
-template <int DIM>
-void launch_sym(const GaussPlan& P, const PointsView& s, const double* gv, double* w, unsigned* err, const int* skip,
-                cudaStream_t st) {
-  constexpr size_t sm = LayoutS<DIM>::total;
+template <int DIM, int NV>
+void launch_sym(const GaussPlan& P, const PointsView& s, const double* gv, double* w, long long vs, unsigned* err,
+                const int* skip, cudaStream_t st) {
+  constexpr size_t sm = LayoutS<DIM, NV>::total;
   static_assert(sm <= 227 * 1024, "k_gauss_sym shared memory");
   static bool attr_set[64] = {false};
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
-    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_sym<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_sym<DIM, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
-  const SumConsts k0 = sum_consts(P.g.sigma, false, LayoutS<DIM>::ET::n);
+  const SumConsts k0 = sum_consts(P.g.sigma, false, LayoutS<DIM, NV>::ET::n);
   const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
-  k_gauss_sym<DIM><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, s.x, s.y, s.z, gv, P.sym_cy.get(),
-                                               s.cell_start, w, P.sym_part.get(), P.sym_pstride, k0, err, skip);
+  k_gauss_sym<DIM, NV><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, s.x, s.y, s.z, gv, vs,
+                                                   P.sym_cy.get(), s.cell_start, w, P.sym_part.get(),
+                                                   P.sym_pstride, P.sym_K, k0, err, skip);
   PRBF_CHECK_LAUNCH();
   const int gb = std::max(1, std::min(ceil_div(s.n, 256), 8 * 152));
-  k_sym_gather<<<gb, 256, 0, st>>>(s.n, P.sym_K, P.sym_pstride, P.sym_part.get(), w, skip);
+  k_sym_gather<<<gb, 256, 0, st>>>(s.n, NV, P.sym_K, P.sym_pstride, P.sym_part.get(), w, vs, skip);
   PRBF_CHECK_LAUNCH();
+}
+
+template <int DIM>
+void launch_sym_nv(const GaussPlan& P, const PointsView& s, const double* gv, double* w, int nv, long long vs,
+                   unsigned* err, const int* skip, cudaStream_t st) {
+  for (int v0 = 0; v0 < nv; v0 += 4) {
+    const double* g0 = gv + v0 * vs;
+    double* w0 = w + v0 * vs;
+    switch (std::min(4, nv - v0)) {
+      case 1: launch_sym<DIM, 1>(P, s, g0, w0, vs, err, skip, st); break;
+      case 2: launch_sym<DIM, 2>(P, s, g0, w0, vs, err, skip, st); break;
+      case 3: launch_sym<DIM, 3>(P, s, g0, w0, vs, err, skip, st); break;
+      default: launch_sym<DIM, 4>(P, s, g0, w0, vs, err, skip, st); break;
+    }
+  }
 }
 
 template <int DIM, int NV, bool BATCH>
@@ -1466,8 +1514,10 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
     plan.f32_ready = true;
   }
   // symmetric FP64 matvec: the same point set on both sides, every cell within one item
-  // (<= kTileT points), 2 nb + 1 mask bits per axis, and the partial slots within 1/8 of
-  // the free device memory
+  // (<= kTileT points), 2 nb + 1 mask bits per axis, at most kSymMaxK partial slots per
+  // point and vector (each product writes and gathers them: the 7 x 7 x 7 window of a 3D
+  // cutoff of 2.8 cells has 171, whose traffic costs more than the halved exponentials
+  // save), and the slots within 1/8 of the free device memory
   if (tgt.x == src.x && tgt.n == src.n && src.n > 0 && 2 * g.nb_trunc + 1 <= kMaskBits && (g.dim == 2 || g.dim == 3)) {
     int* dmax = (int*)ws.get(25, sizeof(int));
     PRBF_CUDA(cudaMemsetAsync(dmax, 0, sizeof(int), s));
@@ -1481,12 +1531,14 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
     const long long pstride = ((long long)src.n + 8 + 31) / 32 * 32;
     size_t free_b = 0, total_b = 0;
     PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const double bytes = (double)K * pstride * sizeof(double) + (double)(src.n + 8) * 8;
-    if (hmax <= kTileT && K >= 1 && bytes <= 0.125 * (double)free_b) {
+    const int nvs = std::max(1, std::min(4, plan.sym_nv));
+    const double bytes = (double)K * nvs * pstride * sizeof(double) + (double)(src.n + 8) * 8;
+    if (hmax <= kTileT && K >= 1 && K <= kSymMaxK && bytes <= 0.125 * (double)free_b) {
       plan.sym_K = K;
+      plan.sym_nv = nvs;
       plan.sym_pstride = pstride;
-      plan.sym_part.reserve((size_t)K * pstride);
-      PRBF_CUDA(cudaMemsetAsync(plan.sym_part.get(), 0, sizeof(double) * (size_t)K * pstride, s));
+      plan.sym_part.reserve((size_t)K * nvs * pstride);
+      PRBF_CUDA(cudaMemsetAsync(plan.sym_part.get(), 0, sizeof(double) * (size_t)K * nvs * pstride, s));
       plan.sym_cy.reserve((size_t)src.n + 8);
       PRBF_CUDA(cudaMemsetAsync(plan.sym_cy.get(), 0, sizeof(unsigned long long) * ((size_t)src.n + 8), s));
       k_cell_y<<<std::max(1, std::min(ceil_div(g.ncell, 256), 8 * 152)), 256, 0, s>>>(g, src.cell_start,
@@ -1520,11 +1572,11 @@ void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s,
   if (P.nitems == 0 || nv <= 0) return;
   if (nv > 1 && (vstride % 2 || vstride < t.n || vstride < s.n))
     throw Error(PRBF_ERR_ARG, "vector stride must be even and cover the points");
-  if (!fp32 && nv == 1 && P.sym_ready && !P.batched && t.x == s.x && t.n == s.n) {
+  if (!fp32 && P.sym_ready && std::min(nv, 4) <= P.sym_nv && !P.batched && t.x == s.x && t.n == s.n) {
     if (P.g.dim == 2)
-      launch_sym<2>(P, s, gv, w, err, skip, st);
+      launch_sym_nv<2>(P, s, gv, w, nv, vstride, err, skip, st);
     else
-      launch_sym<3>(P, s, gv, w, err, skip, st);
+      launch_sym_nv<3>(P, s, gv, w, nv, vstride, err, skip, st);
     return;
   }
   if (P.g.dim == 2) {

@@ -95,6 +95,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   const double t_sorted = now_ms();
   // ---- operator and RASM set-up ----------------------------------------------------------
   S.plan.g = S.pts.g;
+  S.plan.sym_nv = std::min(4, nrhs);  // right-hand sides summed together by the symmetric form
   gauss_plan_dev(S.plan, S.pts.view(), S.pts.view(), c.err.get(), c.ws, c.stream);
   const bool mixed = p.precision == PRBF_PREC_MIXED;
   size_t free_b = 0, total_b = 0;
