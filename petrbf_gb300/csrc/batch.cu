@@ -198,6 +198,11 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   }
   if (!c.batch) c.batch = new BatchState();
   BatchState& B = *c.batch;
+  // the symmetric form's buffers describe the previous call's points (an outer batch whose
+  // ill-conditioned problems are solved by this call reuses the state): off until rebuilt
+  // for these points, after the autotuner
+  B.plan.sym_ready = false;
+  B.plan.sym_nitems = 0;
   B.nprob = nprob;
   B.dim = dim;
   B.n.assign(nprob, 0);
@@ -357,6 +362,10 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   long long pairs_check = 0;
   upload_items(B.plan, make_items(B, sch.tile, &pairs_check), c.stream);
   B.plan.grid = sch.grid;
+  // FP64 sums in the symmetric form where it applies (each exponential for both rows of a
+  // point pair; the autotuned schedule then serves the FP32 sums of the mixed form)
+  gauss_plan_sym_batch(B.plan, hgrids, PointsView{N, B.x.get(), B.y.get(), dim == 3 ? B.z.get() : nullptr, B.cs.get()},
+                       B.hcs, c.stream);
   // one timed Gaussian sum with the chosen schedule, per precision in use (rates reported)
   auto time_sum = [&](bool fp32) {
     cudaEvent_t e0, e1;

@@ -59,6 +59,8 @@ void Ctx::check_device_error(const char* what) {
     if (h & DEV_ERR_TIMEOUT) throw Error(PRBF_ERR_TIMEOUT, std::string(what) + ": bounded device wait gave up");
     if (h & DEV_ERR_CAPACITY) throw Error(PRBF_ERR_CAPACITY, std::string(what) + ": device capacity exceeded");
     if (h & DEV_ERR_FACTOR) throw Error(PRBF_ERR_FACTOR, std::string(what) + ": block factorisation failed");
+    if (h & DEV_ERR_INDEX)
+      throw Error(PRBF_ERR_CAPACITY, std::string(what) + ": a kernel's bounds check caught an index out of range");
   }
 }
 

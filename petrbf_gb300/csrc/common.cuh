@@ -20,6 +20,7 @@ enum : unsigned {
   DEV_ERR_TIMEOUT = 2u,   // a bounded mbarrier wait gave up
   DEV_ERR_CAPACITY = 4u,  // a per-CTA capacity was exceeded
   DEV_ERR_FACTOR = 8u,    // a block factorisation met a non-positive pivot
+  DEV_ERR_INDEX = 16u,    // a kernel's own bounds check caught an index out of range (skipped)
 };
 
 // Host-side exception carrying a status code; converted to an int at the C ABI.

@@ -110,6 +110,9 @@ struct GaussPlan {
   long long sym_pstride = 0;
   DevBuf<double> sym_part;
   DevBuf<unsigned long long> sym_cy;
+  int sym_nitems = 0;      // batches: one item per non-empty cell (else the plan's items)
+  int sym_ncs = 0;         // batches: entries of the global cell starts (else g.ncell + 1)
+  DevBuf<int2> sym_items;
 };
 
 // Builds the work list and the truncation-set sizes; sets plan.pairs / max_trunc. forms:
@@ -120,6 +123,10 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
 // FP32 form's source data of a batch (each problem with its own grid and scale, grids with
 // their first global cell); sets plan.f32_ready when every grid qualifies.
 void gauss_plan_f32_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src, cudaStream_t s);
+// Symmetric FP64 form of a batch (every grid with the same window, every cell <= 128
+// points; hcs: the global cell starts on the host); false when it does not apply.
+bool gauss_plan_sym_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src,
+                          const std::vector<int>& hcs, cudaStream_t s);
 // w[i] = sum_{j in trunc(cell(i))} g[j] exp(-|t_i - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2)
 // for all sorted targets i; g must be a padded device vector of src.n (+2) entries.
 // w = A g for nv weight vectors at stride vstride (even; vectors padded as the sources)

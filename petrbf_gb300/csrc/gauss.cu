@@ -771,8 +771,8 @@ struct LayoutS {
 // Range r of c1's walk: 0 = c1 itself; 1 = the cells above c1 in its column; then the
 // columns to its right (jy0 .. jy1) in its plane; then (3D) every column of the planes
 // above. Sorted positions [a, b), cell offsets dx, dz from c1.
-__device__ __forceinline__ void sym_range(const Grid& g, const int* __restrict__ cs, int r, int c1, int ix, int iy,
-                                          int iz, int jx0, int jx1, int jy0, int jy1, int& a, int& b, int& dx,
+__device__ __forceinline__ void sym_range(const Grid& g, const int* __restrict__ cs, int ncs, int r, int c1, int ix,
+                                          int iy, int iz, int jx0, int jx1, int jy0, int jy1, int& a, int& b, int& dx,
                                           int& dz) {
   const int cb = g.cbase;
   if (r == 0) {
@@ -800,20 +800,25 @@ __device__ __forceinline__ void sym_range(const Grid& g, const int* __restrict__
   }
   dx = cx - ix;
   dz = cz - iz;
-  if (y0 > jy1) {
-    a = b = 0;
+  const int ca = cb + cell_of(g, cx, y0, cz), ce = cb + cell_of(g, cx, jy1, cz) + 1;
+  if (y0 > jy1 || ca < 0 || ce >= ncs) {  // (out-of-range cells: the caller's bounds check)
+    a = b = y0 > jy1 ? 0 : -1;
     return;
   }
-  a = cs[cb + cell_of(g, cx, y0, cz)];
-  b = cs[cb + cell_of(g, cx, jy1, cz) + 1];
+  a = cs[ca];
+  b = cs[ce];
 }
 
-template <int DIM, int NV>
+// BATCH: as k_gauss (the cell indexes a concatenation of grids, stopped problems skipped);
+// every problem's window has the same K.
+template <int DIM, int NV, bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_gauss_sym(
-    Grid g, const int2* __restrict__ items, int nitems, const double* __restrict__ sx,
+    Grid g0, const Grid* __restrict__ grids, const int* __restrict__ cprob, SegSkip seg,
+    const int2* __restrict__ items, int nitems, const double* __restrict__ sx,
     const double* __restrict__ sy, const double* __restrict__ sz, const double* __restrict__ sg, long long vs,
     const unsigned long long* __restrict__ pcy, const int* __restrict__ cs, double* __restrict__ w,
-    double* __restrict__ part, long long pstride, int K, SumConsts kc, unsigned* err, const int* __restrict__ skip) {
+    double* __restrict__ part, long long pstride, int K, int n, int ncs, SumConsts k0, unsigned* err,
+    const int* __restrict__ skip) {
   if (skip && *skip) return;
   using Lay = LayoutS<DIM, NV>;
   using ET = typename Lay::ET;
@@ -844,16 +849,31 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
   if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
   const int G = gridDim.x;
-  const int nb = g.nb_trunc, W = 2 * nb + 1;
-  const double L = g.trunc_len, kexp = kc.kexp;
 
   for (int round = 0; (long long)round * G < nitems; round++) {
     const int it = (round & 1) ? round * G + (G - 1 - (int)blockIdx.x) : round * G + (int)blockIdx.x;
     if (it >= nitems) continue;
     const int c1 = items[it].x, t0 = items[it].y;
+    if (c1 < 0 || c1 + 1 >= ncs) {  // bounds check: record and skip the item
+      if (threadIdx.x == 0) atomicOr(err, DEV_ERR_INDEX);
+      continue;
+    }
+    Grid g = g0;
+    SumConsts kc = k0;
+    if constexpr (BATCH) {
+      if (seg.cell_done(c1)) continue;  // a stopped problem (uniform over the CTA)
+      g = grids[cprob[c1]];
+      kc = sum_consts(g.sigma, false, ET::n);
+    }
+    const int nb = g.nb_trunc, W = 2 * nb + 1;
+    const double L = g.trunc_len, kexp = kc.kexp;
     const int nt = min(kTileT, cs[c1 + 1] - t0);  // every cell has at most kTileT points here
+    if (t0 < 0 || nt < 0 || t0 + nt > n) {  // bounds check: record and skip the item
+      if (threadIdx.x == 0) atomicOr(err, DEV_ERR_INDEX);
+      continue;
+    }
     int ix, iy, iz;
-    cell_xyz(g, c1, ix, iy, iz);
+    cell_xyz(g, c1 - g.cbase, ix, iy, iz);
     const double xc = centre_coord(g.xmin, ix, g.box);
     const double yc = centre_coord(g.ymin, iy, g.box);
     const double zc = DIM == 3 ? centre_coord(g.zmin, iz, g.box) : 0.0;
@@ -1016,15 +1036,25 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
 #pragma unroll
         for (int m = 0; m < SPL; m++) {
           const int idx = s0 + lane + m * kWarps * 32;
-          if (valid[m] && self[m])  // row idx of c1 itself
+          if (valid[m] && self[m]) {  // row idx of c1 itself
+            if (idx < nt) {
 #pragma unroll
-            for (int v = 0; v < NV; v++) acct[(wid * NV + v) * kTileT + idx] += accs[m][v];
+              for (int v = 0; v < NV; v++) acct[(wid * NV + v) * kTileT + idx] += accs[m][v];
+            } else {
+              atomicOr(err, DEV_ERR_INDEX);
+            }
+          }
           if (valid[m] && !self[m]) {
             const int ddx = kx[m] - nb, ddy = ky[m] - kMaskY - nb, ddz = DIM == 3 ? kz[m] - kMaskZ - nb : 0;
             const int key = (ddz * W + ddx) * W + ddy;  // > 0 for the upper half of the window
+            const int jj = cj[idx];
+            if (key >= 1 && key <= K && jj >= 0 && jj < n) {
 #pragma unroll
-            for (int v = 0; v < NV; v++)
-              part[((long long)v * K + key - 1) * pstride + cj[idx]] = accs[m][v] * kc.norm;
+              for (int v = 0; v < NV; v++)
+                part[((long long)v * K + key - 1) * pstride + jj] = accs[m][v] * kc.norm;
+            } else {
+              atomicOr(err, DEV_ERR_INDEX);
+            }
           }
         }
         __syncwarp();
@@ -1040,7 +1070,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
         unsigned bytes = 0;
         while (r < nranges && np < kMaxPieces && RC - used >= 4) {
           int a, b, ddx, ddz;
-          sym_range(g, cs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a, b, ddx, ddz);
+          sym_range(g, cs, ncs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a, b, ddx, ddz);
+          if (a < 0 || b > n || a > b) {  // bounds check: record and skip the range
+            atomicOr(err, DEV_ERR_INDEX);
+            a = b = 0;
+          }
           int s = p < 0 ? a : p;
           if (s >= b) {
             r++;
@@ -1110,7 +1144,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
         const Piece pc = pieces[q];
         const int r = prange[q];
         int a_, b_, ddx, ddz;
-        sym_range(g, cs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a_, b_, ddx, ddz);
+        sym_range(g, cs, ncs, r, c1, ix, iy, iz, jx0, jx1, jy0, jy1, a_, b_, ddx, ddz);
         for (int e0 = 0; e0 < pc.count; e0 += kThreads) {
           const int e = e0 + tid;
           bool in = false;
@@ -1130,6 +1164,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
               in = true;  // the centre cell, unconditionally (2d/get_trunc.h:31-39)
             } else {
               const int ddy = (int)__double_as_longlong(raw[(DIM + NV) * RC + ro]) - iy;
+              if (ddy < -nb || ddy > nb || ddx < 0 || ddx > nb) atomicOr(err, DEV_ERR_INDEX);
               // j in T(c1): the box test against c1's centre (2d/get_trunc.h:63)
               bool fij = fabs(vx - xc) < L && fabs(vy - yc) < L;
               if (DIM == 3) fij = fij && fabs(vz - zc) < L;
@@ -1349,24 +1384,39 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
   PRBF_CHECK_LAUNCH();
 }
 
-template <int DIM, int NV>
-void launch_sym(const GaussPlan& P, const PointsView& s, const double* gv, double* w, long long vs, unsigned* err,
-                const int* skip, cudaStream_t st) {
+template <int DIM, int NV, bool BATCH>
+void launch_sym_k(const GaussPlan& P, const PointsView& s, const double* gv, double* w, long long vs, unsigned* err,
+                  const int* skip, cudaStream_t st) {
   constexpr size_t sm = LayoutS<DIM, NV>::total;
   static_assert(sm <= 227 * 1024, "k_gauss_sym shared memory");
   static bool attr_set[64] = {false};
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
-    PRBF_CUDA(cudaFuncSetAttribute(k_gauss_sym<DIM, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PRBF_CUDA(
+        cudaFuncSetAttribute(k_gauss_sym<DIM, NV, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     if (dev < 64) attr_set[dev] = true;
   }
   const SumConsts k0 = sum_consts(P.g.sigma, false, LayoutS<DIM, NV>::ET::n);
-  const int grid = P.grid > 0 ? std::min(P.grid, P.nitems) : P.nitems;
-  k_gauss_sym<DIM, NV><<<grid, kThreads, sm, st>>>(P.g, P.items.get(), P.nitems, s.x, s.y, s.z, gv, vs,
-                                                   P.sym_cy.get(), s.cell_start, w, P.sym_part.get(),
-                                                   P.sym_pstride, P.sym_K, k0, err, skip);
+  // one item per cell: the plan's own items (cells within one tile) or, for a batch, its
+  // per-cell list
+  const int2* it = P.sym_nitems > 0 ? P.sym_items.get() : P.items.get();
+  const int nit = P.sym_nitems > 0 ? P.sym_nitems : P.nitems;
+  const int grid = P.sym_nitems > 0 ? nit : (P.grid > 0 ? std::min(P.grid, nit) : nit);
+  k_gauss_sym<DIM, NV, BATCH><<<grid, kThreads, sm, st>>>(P.g, P.grids.get(), P.cprob.get(), P.seg, it, nit, s.x,
+                                                          s.y, s.z, gv, vs, P.sym_cy.get(), s.cell_start, w,
+                                                          P.sym_part.get(), P.sym_pstride, P.sym_K, s.n,
+                                                          P.sym_ncs > 0 ? P.sym_ncs : P.g.ncell + 1, k0, err, skip);
   PRBF_CHECK_LAUNCH();
+}
+
+template <int DIM, int NV>
+void launch_sym(const GaussPlan& P, const PointsView& s, const double* gv, double* w, long long vs, unsigned* err,
+                const int* skip, cudaStream_t st) {
+  if (P.batched)
+    launch_sym_k<DIM, NV, true>(P, s, gv, w, vs, err, skip, st);
+  else
+    launch_sym_k<DIM, NV, false>(P, s, gv, w, vs, err, skip, st);
   const int gb = std::max(1, std::min(ceil_div(s.n, 256), 8 * 152));
   k_sym_gather<<<gb, 256, 0, st>>>(s.n, NV, P.sym_K, P.sym_pstride, P.sym_part.get(), w, vs, skip);
   PRBF_CHECK_LAUNCH();
@@ -1504,6 +1554,8 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
   // FP32 form's source data
   plan.f32_ready = false;
   plan.sym_ready = false;
+  plan.sym_nitems = 0;
+  plan.sym_ncs = 0;
   if (!forms) return;
   if (f32_grid_ok(g) && src.n > 0) {
     alloc_f32(plan, g.dim, src.n, s);
@@ -1549,6 +1601,51 @@ void gauss_plan_dev(GaussPlan& plan, const PointsView& tgt, const PointsView& sr
   }
 }
 
+bool gauss_plan_sym_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src,
+                          const std::vector<int>& hcs, cudaStream_t s) {
+  plan.sym_ready = false;
+  plan.sym_nitems = 0;
+  if (grids.empty() || src.n <= 0) return false;
+  const int nb = grids[0].nb_trunc, dim = grids[0].dim;
+  for (const Grid& g : grids)
+    if (g.nb_trunc != nb || 2 * nb + 1 > kMaskBits) return false;
+  const int W = 2 * nb + 1;
+  const int K = dim == 2 ? (W * W - 1) / 2 : (W * W * W - 1) / 2;
+  if (K < 1 || K > kSymMaxK) return false;
+  // one item per non-empty cell, each cell within one item; largest first
+  std::vector<int2> its;
+  const int ncell = (int)hcs.size() - 1;
+  for (int c = 0; c < ncell; c++) {
+    const int m = hcs[c + 1] - hcs[c];
+    if (m > kTileT) return false;
+    if (m > 0) its.push_back(make_int2(c, hcs[c]));
+  }
+  std::stable_sort(its.begin(), its.end(),
+                   [&](const int2& a, const int2& b) { return hcs[a.x + 1] - hcs[a.x] > hcs[b.x + 1] - hcs[b.x]; });
+  const long long pstride = ((long long)src.n + 8 + 31) / 32 * 32;
+  size_t free_b = 0, total_b = 0;
+  PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if ((double)K * pstride * sizeof(double) + (double)(src.n + 8) * 8 > 0.125 * (double)free_b) return false;
+  plan.sym_K = K;
+  plan.sym_nv = 1;
+  plan.sym_ncs = (int)hcs.size();
+  plan.sym_pstride = pstride;
+  plan.sym_part.reserve((size_t)K * pstride);
+  PRBF_CUDA(cudaMemsetAsync(plan.sym_part.get(), 0, sizeof(double) * (size_t)K * pstride, s));
+  plan.sym_cy.reserve((size_t)src.n + 8);
+  PRBF_CUDA(cudaMemsetAsync(plan.sym_cy.get(), 0, sizeof(unsigned long long) * ((size_t)src.n + 8), s));
+  for (const Grid& g : grids)
+    k_cell_y<<<std::max(1, std::min(ceil_div(g.ncell, 256), 8 * 152)), 256, 0, s>>>(g, src.cell_start + g.cbase,
+                                                                                  plan.sym_cy.get());
+  PRBF_CHECK_LAUNCH();
+  plan.sym_items.reserve(std::max<size_t>(its.size(), 1));
+  PRBF_CUDA(cudaMemcpyAsync(plan.sym_items.get(), its.data(), sizeof(int2) * its.size(), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  plan.sym_nitems = (int)its.size();
+  plan.sym_ready = true;
+  return true;
+}
+
 void gauss_plan_f32_batch(GaussPlan& plan, const std::vector<Grid>& grids, const PointsView& src, cudaStream_t s) {
   plan.f32_ready = false;
   if (src.n <= 0) return;
@@ -1572,7 +1669,7 @@ void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s,
   if (P.nitems == 0 || nv <= 0) return;
   if (nv > 1 && (vstride % 2 || vstride < t.n || vstride < s.n))
     throw Error(PRBF_ERR_ARG, "vector stride must be even and cover the points");
-  if (!fp32 && P.sym_ready && std::min(nv, 4) <= P.sym_nv && !P.batched && t.x == s.x && t.n == s.n) {
+  if (!fp32 && P.sym_ready && std::min(nv, 4) <= P.sym_nv && t.x == s.x && t.n == s.n) {
     if (P.g.dim == 2)
       launch_sym_nv<2>(P, s, gv, w, nv, vstride, err, skip, st);
     else
