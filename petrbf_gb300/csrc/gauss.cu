@@ -732,8 +732,9 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
 // ---- FP64 matvec with each exponential used for both rows --------------------------
 // When the targets are the sources (the matvec of the solve), the pair (i, j) enters row i
 // when j is in T(c(i)) and row j when i is in T(c(j)), with the same exponential. One CTA
-// per cell c1 (at most kTileT points): its own points against themselves (row i only:
-// the centre cell is taken unconditionally), then against the points of the upper half of
+// per cell c1 (at most kTileT points): its own points against themselves (each pair once,
+// both rows inside c1: the centre cell is taken unconditionally), then against the points
+// of the upper half of
 // its neighbour window -- the window cells with a larger cell index -- computing each
 // exponential once and adding it to row i when j is in T(c1) (the FP64 box test against
 // c1's centre, as the reference's) and to row j when i is in T(c(j)) (the target's box-test
@@ -744,7 +745,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
 // (distance 4, exponential 6, two accumulations) against 2 x 11.
 // Lanes own sources (SPL at a time), each warp walks all targets in groups of kGroup, and
 // the per-target sums go to per-warp rows of shared memory that are added in warp order
-// at the end: the result does not depend on scheduling.
+// at the end: the result does not depend on scheduling. Every index the kernel forms for a
+// global access is bounds-checked; an out-of-range one sets DEV_ERR_INDEX and is skipped.
 constexpr int kSymRC = 512;   // staged sources per fill
 constexpr int kSymMaxK = 32;  // partial slots per point and vector (upper window cells)
 
