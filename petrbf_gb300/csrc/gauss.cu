@@ -1166,7 +1166,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
               in = true;  // the centre cell, unconditionally (2d/get_trunc.h:31-39)
             } else {
               const int ddy = (int)__double_as_longlong(raw[(DIM + NV) * RC + ro]) - iy;
-              if (ddy < -nb || ddy > nb || ddx < 0 || ddx > nb) atomicOr(err, DEV_ERR_INDEX);
+              // (the planes above a 3D cell take every column of the window: dx may be negative)
+              if (ddy < -nb || ddy > nb || ddx < -nb || ddx > nb || ddz < 0 || ddz > nb) atomicOr(err, DEV_ERR_INDEX);
               // j in T(c1): the box test against c1's centre (2d/get_trunc.h:63)
               bool fij = fabs(vx - xc) < L && fabs(vy - yc) < L;
               if (DIM == 3) fij = fij && fabs(vz - zc) < L;
