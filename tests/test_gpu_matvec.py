@@ -190,3 +190,20 @@ def test_full_size_matvec_rows_against_oracle(which):
     scale = np.max(np.abs(yo))
     assert np.max(np.abs(y[k] - yo)) <= 1e-12 * scale
     assert np.max(np.abs(y32[k] - yo)) <= 1e-4 * scale
+
+
+def test_symmetric_form_where_it_applies():
+    # 2D config-1 geometry (5 x 5 window: 12 upper cells): the FP64 product takes the
+    # symmetric form (sum + gather); a 3D 7 x 7 x 7 window (171 upper cells) keeps the
+    # one-sided kernel; FP32 products are the conversion and the sum
+    p = W.config1()
+    with Context(dim=2, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+                 sigma_trunc=p.sigma_trunc) as c:
+        c.matvec_setup(p.x, p.y)
+        assert c.matvec_kernels() == (2, True)
+        assert c.matvec_kernels(fp32=True) == (2, False)
+    x, y, z, h = W.lattice_3d(12, jitter=0.25, seed=1)
+    with Context(dim=3, sigma=h / 0.8, nsigma_box=3, sigma_buffer=7, sigma_trunc=17) as c:
+        c.matvec_setup(x, y, z)
+        assert c.matvec_info()["nb_trunc"] == 3
+        assert c.matvec_kernels() == (1, False)
