@@ -170,6 +170,22 @@ def test_solve_jittered_and_multiple_rhs():
         assert _rel(g[:, k], go) <= RTOL_WEIGHTS
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_six_right_hand_sides(precision):
+    # more right-hand sides than one launch carries (four): the sums run in chunks, each
+    # right-hand side converges to the oracle's answer
+    p = W.lamb_oseen_2d(40, jitter=0.25, seed=9)
+    fs = np.stack([p.f * (1 + 0.1 * k) + np.sin((k + 1) * p.x) * np.cos(2 * p.y) for k in range(6)], axis=1)
+    rtol = 1e-16 if precision == "fp64" else 1e-14
+    with _ctx(p, rtol=rtol, max_it=400, precision=precision) as c:
+        g, st = c.interpolate(p.x, p.y, None, fs)
+    assert st.reason > 0
+    for k in range(6):
+        go, _, reason = O.rbf_interpolation(p.x, p.y, None, fs[:, k], *p.params(), rtol=1e-16, max_it=400)
+        assert reason == 2
+        assert _rel(g[:, k], go) <= (RTOL_WEIGHTS if precision == "fp64" else 1e-8)
+
+
 def test_solve_3d_small_matches_oracle():
     # 3D jittered lattices need a wider overlap than one 2-sigma cell for RASM to work:
     # sigma_buffer = nsigma_box + 8 (4 sigma on each side); cutoff 7 sigma past the cell
