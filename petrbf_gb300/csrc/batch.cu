@@ -604,20 +604,7 @@ extern "C" {
 
 int prbf_batch_interpolate(prbf_ctx* ctx, int nprob, const prbf_problem* probs, int* its_out, int* reason_out,
                            prbf_batch_stats* stats) {
-  if (!ctx) return PRBF_ERR_ARG;
-  Ctx& c = ctx->c;
-  try {
-    c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(c.device));
-    batch_interpolate(c, nprob, probs, its_out, reason_out, stats);
-    return PRBF_OK;
-  } catch (const Error& e) {
-    c.last_error = e.what();
-    return e.status;
-  } catch (const std::exception& e) {
-    c.last_error = e.what();
-    return PRBF_ERR_ARG;
-  }
+  return ctx_call(ctx, [&](Ctx& c) { batch_interpolate(c, nprob, probs, its_out, reason_out, stats); });
 }
 
 }  // extern "C"

@@ -100,26 +100,6 @@ using namespace prbf;
 
 namespace {
 
-template <class F>
-int guarded(prbf_ctx* ctx, F&& f) {
-  if (!ctx) return PRBF_ERR_ARG;
-  try {
-    ctx->c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(ctx->c.device));
-    f(ctx->c);
-    return PRBF_OK;
-  } catch (const Error& e) {
-    ctx->c.last_error = e.what();
-    return e.status;
-  } catch (const std::bad_alloc&) {
-    ctx->c.last_error = "host allocation failed";
-    return PRBF_ERR_CAPACITY;
-  } catch (const std::exception& e) {
-    ctx->c.last_error = e.what();
-    return PRBF_ERR_ARG;
-  }
-}
-
 void check_n(int n) {
   if (n <= 0 || n > (1 << 30)) throw Error(PRBF_ERR_ARG, "point count must be in [1, 2^30]");
 }
@@ -228,11 +208,11 @@ const char* prbf_last_error(const prbf_ctx* ctx) { return ctx ? ctx->c.last_erro
 void* prbf_ctx_stream(prbf_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
 
 int prbf_ctx_synchronize(prbf_ctx* ctx) {
-  return guarded(ctx, [&](Ctx& c) { PRBF_CUDA(cudaStreamSynchronize(c.stream)); });
+  return ctx_call(ctx, [&](Ctx& c) { PRBF_CUDA(cudaStreamSynchronize(c.stream)); });
 }
 
 int prbf_selftest_wait_timeout(prbf_ctx* ctx, unsigned max_polls) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (max_polls == 0 || max_polls > (1u << 20)) throw Error(PRBF_ERR_ARG, "max_polls must be in [1, 2^20]");
     k_selftest_wait<<<1, 32, 0, c.stream>>>(max_polls, c.err.get());
     PRBF_CHECK_LAUNCH();
@@ -241,7 +221,7 @@ int prbf_selftest_wait_timeout(prbf_ctx* ctx, unsigned max_polls) {
 }
 
 int prbf_matvec_setup(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     check_n(n);
     c.mv_ready = false;
     DevBuf<double> ux, uy, uz;
@@ -262,7 +242,7 @@ int prbf_matvec_setup(prbf_ctx* ctx, int n, const double* x, const double* y, co
 }
 
 int prbf_matvec_dev(prbf_ctx* ctx, const double* xin, double* yout, int flags) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (!xin || !yout) throw Error(PRBF_ERR_ARG, "null vector");
     int n = c.mv_pts.n;
@@ -281,7 +261,7 @@ int prbf_matvec_dev(prbf_ctx* ctx, const double* xin, double* yout, int flags) {
 }
 
 int prbf_matvec(prbf_ctx* ctx, const double* xin, double* yout) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (!xin || !yout) throw Error(PRBF_ERR_ARG, "null vector");
     int n = c.mv_pts.n;
@@ -296,7 +276,7 @@ int prbf_matvec(prbf_ctx* ctx, const double* xin, double* yout) {
 }
 
 int prbf_matvec_kernels(prbf_ctx* ctx, int fp32, int* kernels, int* symmetric) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     const bool sym = !fp32 && c.mv_plan.sym_ready;
     if (kernels) *kernels = fp32 ? (c.mv_plan.f32_ready ? 2 : 1) : (sym ? 2 : 1);
@@ -305,7 +285,7 @@ int prbf_matvec_kernels(prbf_ctx* ctx, int fp32, int* kernels, int* symmetric) {
 }
 
 int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     const Grid& g = c.mv_pts.g;
     if (ints7) {
@@ -321,7 +301,7 @@ int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs)
 }
 
 int prbf_get_permutation(prbf_ctx* ctx, int* perm) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (!perm) throw Error(PRBF_ERR_ARG, "null output");
     PRBF_CUDA(cudaMemcpyAsync(perm, c.mv_pts.perm.get(), sizeof(int) * c.mv_pts.n, cudaMemcpyDeviceToHost, c.stream));
@@ -330,7 +310,7 @@ int prbf_get_permutation(prbf_ctx* ctx, int* perm) {
 }
 
 int prbf_get_cell_start(prbf_ctx* ctx, int* cs) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (!cs) throw Error(PRBF_ERR_ARG, "null output");
     PRBF_CUDA(cudaMemcpyAsync(cs, c.mv_pts.cs.get(), sizeof(int) * ((size_t)c.mv_pts.g.ncell + 1),
@@ -340,7 +320,7 @@ int prbf_get_cell_start(prbf_ctx* ctx, int* cs) {
 }
 
 int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (!counts) throw Error(PRBF_ERR_ARG, "null output");
     PRBF_CUDA(cudaMemcpyAsync(counts, c.mv_plan.trunc_cnt.get(), sizeof(int) * c.mv_pts.g.ncell,
@@ -351,7 +331,7 @@ int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts) {
 
 int prbf_evaluate(prbf_ctx* ctx, int nt, const double* xt, const double* yt, const double* zt, int ns,
                   const double* xs, const double* ys, const double* zs, const double* gs, double* w_out) {
-  return guarded(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     check_n(nt);
     check_n(ns);
     if (!gs || !w_out) throw Error(PRBF_ERR_ARG, "null array");

@@ -440,5 +440,7 @@ extern "C" int prbf_cell_sort_static(int dim, int n, const double* x, const doub
     return PRBF_OK;
   } catch (const Error& e) {
     return e.status;
+  } catch (const std::exception&) {
+    return PRBF_ERR_ARG;
   }
 }

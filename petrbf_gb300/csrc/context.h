@@ -1,7 +1,9 @@
 // context.h -- the prbf_ctx behind the C ABI and the host-side helpers shared by the
 // C-ABI translation units.
 #pragma once
+#include <exception>
 #include <memory>
+#include <new>
 #include <string>
 
 #include "device.h"
@@ -63,3 +65,31 @@ void bbox_host(Ctx& c, int n, const double* dx, const double* dy, const double* 
 struct prbf_ctx {
   prbf::Ctx c;
 };
+
+namespace prbf {
+
+// Body of a C-ABI entry point on a context: selects the context's device, runs f(ctx->c)
+// and turns every exception into a status, with its message in last_error (no exception
+// crosses the C ABI).
+template <class F>
+int ctx_call(prbf_ctx* ctx, F&& f) {
+  if (!ctx) return PRBF_ERR_ARG;
+  Ctx& c = ctx->c;
+  try {
+    c.last_error.clear();
+    PRBF_CUDA(cudaSetDevice(c.device));
+    f(c);
+    return PRBF_OK;
+  } catch (const Error& e) {
+    c.last_error = e.what();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    c.last_error = "host allocation failed";
+    return PRBF_ERR_CAPACITY;
+  } catch (const std::exception& e) {
+    c.last_error = e.what();
+    return PRBF_ERR_ARG;
+  }
+}
+
+}  // namespace prbf

@@ -82,24 +82,9 @@ int mlp_guard(prbf_mlp* m, F&& f) {
     return PRBF_OK;
   } catch (const Error& e) {
     return e.status;
+  } catch (const std::bad_alloc&) {
+    return PRBF_ERR_CAPACITY;
   } catch (const std::exception&) {
-    return PRBF_ERR_ARG;
-  }
-}
-
-template <class F>
-int ctx_guard(prbf_ctx* ctx, F&& f) {
-  if (!ctx) return PRBF_ERR_ARG;
-  try {
-    ctx->c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(ctx->c.device));
-    f(ctx->c);
-    return PRBF_OK;
-  } catch (const Error& e) {
-    ctx->c.last_error = e.what();
-    return e.status;
-  } catch (const std::exception& e) {
-    ctx->c.last_error = e.what();
     return PRBF_ERR_ARG;
   }
 }
@@ -246,7 +231,7 @@ int prbf_mlp_train(prbf_mlp* m, int n, const float* X, const float* T, const flo
 
 int prbf_guess_patches(prbf_ctx* ctx, int n, const double* x, const double* y, const double* f, const double* g,
                        float* X, float* scale, float* T, float* M, int* npatch) {
-  return ctx_guard(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (c.p.dim != 2) throw Error(PRBF_ERR_ARG, "the learned guess is 2D");
     if (n <= 0 || !x || !y || !f || !npatch) throw Error(PRBF_ERR_ARG, "bad arguments");
     DevBuf<double> ux, uy, uf, ug, ff, gf;
@@ -287,7 +272,7 @@ int prbf_guess_patches(prbf_ctx* ctx, int n, const double* x, const double* y, c
 }
 
 int prbf_guess_set_weights(prbf_ctx* ctx, const float* w) {
-  return ctx_guard(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!w) throw Error(PRBF_ERR_ARG, "null weights");
     if (!c.guess) c.guess = new Mlp();
     c.guess->set_weights(w, c.stream);
@@ -296,7 +281,7 @@ int prbf_guess_set_weights(prbf_ctx* ctx, const float* w) {
 }
 
 int prbf_guess_eval(prbf_ctx* ctx, int n, const double* x, const double* y, const double* f, double* g0) {
-  return ctx_guard(ctx, [&](Ctx& c) {
+  return ctx_call(ctx, [&](Ctx& c) {
     if (c.p.dim != 2) throw Error(PRBF_ERR_ARG, "the learned guess is 2D");
     if (!c.guess || !c.guess->ready) throw Error(PRBF_ERR_STATE, "no learned-guess weights installed");
     if (n <= 0 || !x || !y || !f || !g0) throw Error(PRBF_ERR_ARG, "bad arguments");

@@ -14,6 +14,7 @@
 // non-finite one, hands the call to the plain form (FP64 blocks, FP64 GMRES from zero).
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -115,6 +116,8 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   const int nv = nrhs;
   const long long ldn = ((long long)n + 4 + 31) / 32 * 32;
   const long long len_all = ldn * nv + 32;
+  if (ldn * nv > (long long)INT_MAX)
+    throw Error(PRBF_ERR_CAPACITY, "points x right-hand sides must stay below 2^31 (solve in several calls)");
   S.op64.plan = S.op32.plan = &S.plan;
   S.op64.v = S.op32.v = S.pts.view();
   S.op64.rasm = S.op32.rasm = &S.rasm;
@@ -345,31 +348,16 @@ extern "C" {
 
 int prbf_interpolate(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z, const double* f, int nrhs,
                      double* g_out, prbf_stats* stats) {
-  if (!ctx) return PRBF_ERR_ARG;
-  Ctx& c = ctx->c;
-  try {
-    c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(c.device));
+  return ctx_call(ctx, [&](Ctx& c) {
     if (n <= 0 || n > (1 << 30)) throw Error(PRBF_ERR_ARG, "point count must be in [1, 2^30]");
     if (!x || !y || (c.p.dim == 3 && !z) || !f || !g_out || nrhs <= 0)
       throw Error(PRBF_ERR_ARG, "null array or nrhs <= 0");
     interpolate(c, n, x, y, z, f, nrhs, g_out, stats);
-    return PRBF_OK;
-  } catch (const Error& e) {
-    c.last_error = e.what();
-    return e.status;
-  } catch (const std::exception& e) {
-    c.last_error = e.what();
-    return PRBF_ERR_ARG;
-  }
+  });
 }
 
 int prbf_pc_setup(prbf_ctx* ctx, int precision) {
-  if (!ctx) return PRBF_ERR_ARG;
-  Ctx& c = ctx->c;
-  try {
-    c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(c.device));
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.mv_ready) throw Error(PRBF_ERR_STATE, "prbf_matvec_setup has not been called");
     if (precision != PRBF_PREC_FP64 && precision != PRBF_PREC_MIXED) throw Error(PRBF_ERR_ARG, "bad precision");
     if (!c.solve) c.solve = new SolveState();
@@ -382,19 +370,11 @@ int prbf_pc_setup(prbf_ctx* ctx, int precision) {
     rasm_set_apply_smem(c.solve->pc);
     c.check_device_error("RASM set-up");
     c.solve->pc_ready = true;
-    return PRBF_OK;
-  } catch (const Error& e) {
-    c.last_error = e.what();
-    return e.status;
-  }
+  });
 }
 
 int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z) {
-  if (!ctx) return PRBF_ERR_ARG;
-  Ctx& c = ctx->c;
-  try {
-    c.last_error.clear();
-    PRBF_CUDA(cudaSetDevice(c.device));
+  return ctx_call(ctx, [&](Ctx& c) {
     if (!c.solve || !c.solve->pc_ready) throw Error(PRBF_ERR_STATE, "prbf_pc_setup has not been called");
     if (!r || !z) throw Error(PRBF_ERR_ARG, "null vector");
     int n = c.mv_pts.n;
@@ -404,11 +384,7 @@ int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z) {
     scatter_dev(n, c.mv_pts.perm.get(), c.vout.get(), c.vtmp.get(), c.stream);
     PRBF_CUDA(cudaMemcpyAsync(z, c.vtmp.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
     c.check_device_error("pc apply");
-    return PRBF_OK;
-  } catch (const Error& e) {
-    c.last_error = e.what();
-    return e.status;
-  }
+  });
 }
 
 // 3d/wrapper.cxx:20-105 with the same argument meaning. It creates its own context on
@@ -433,6 +409,10 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
   // the particle field is evaluated at the grid points first when the first grid point
   // differs from the first particle (3d/wrapper.cxx:93-95)
   if (np > 0 && xp && std::fabs(xg[0] - xp[0]) > kEpsf) {
+    if (!yp || !zp || !gp) {
+      prbf_ctx_destroy(ctx);
+      return PRBF_ERR_ARG;
+    }
     std::vector<double> xj(xp, xp + np), yj(yp, yp + np), zj(zp, zp + np), gj(gp, gp + np);
     st = prbf_evaluate(ctx, ng, xi.data(), yi.data(), zi.data(), np, xj.data(), yj.data(), zj.data(), gj.data(),
                        wi.data());
