@@ -559,7 +559,15 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
       ~Restore() { p.precision = prec; }
     } restore{c.p, c.p.precision};
     c.p.precision = PRBF_PREC_FP64;
-    batch_interpolate(c, (int)sub.size(), sub.data(), sits.data(), sreason.data(), &sst);
+    try {
+      batch_interpolate(c, (int)sub.size(), sub.data(), sits.data(), sreason.data(), &sst);
+    } catch (const Error& e) {
+      // a problem of the FP64 batch stopped short of the tolerance: its iterations, reason
+      // and the batch statistics are already written, and the status is raised below
+      if (e.status != PRBF_ERR_NOT_CONVERGED && e.status != PRBF_ERR_BREAKDOWN && e.status != PRBF_ERR_NAN &&
+          e.status != PRBF_ERR_DIVERGED)
+        throw;
+    }
     for (size_t k = 0; k < sub_idx.size(); k++) {
       its[sub_idx[k]] += sits[k];
       reason[sub_idx[k]] = sreason[k];
