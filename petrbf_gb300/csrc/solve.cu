@@ -395,6 +395,10 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
   (void)argc;
   (void)argv;
   if (ng <= 0 || !xg || !yg || !zg || !wg) return PRBF_ERR_ARG;
+  // the particle field is evaluated at the grid points first when the first grid point
+  // differs from the first particle (3d/wrapper.cxx:93-95)
+  const bool eval_first = np > 0 && xp && std::fabs(xg[0] - xp[0]) > kEpsf;
+  if (eval_first && (!yp || !zp || !gp)) return PRBF_ERR_ARG;
   prbf_params p;
   prbf_params_default(&p);
   p.dim = 3;
@@ -406,13 +410,7 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
   int st = prbf_ctx_create(&p, &ctx);
   if (st) return st;
   std::vector<double> xi(xg, xg + ng), yi(yg, yg + ng), zi(zg, zg + ng), wi(wg, wg + ng), gi(ng);
-  // the particle field is evaluated at the grid points first when the first grid point
-  // differs from the first particle (3d/wrapper.cxx:93-95)
-  if (np > 0 && xp && std::fabs(xg[0] - xp[0]) > kEpsf) {
-    if (!yp || !zp || !gp) {
-      prbf_ctx_destroy(ctx);
-      return PRBF_ERR_ARG;
-    }
+  if (eval_first) {
     std::vector<double> xj(xp, xp + np), yj(yp, yp + np), zj(zp, zp + np), gj(gp, gp + np);
     st = prbf_evaluate(ctx, ng, xi.data(), yi.data(), zi.data(), np, xj.data(), yj.data(), zj.data(), gj.data(),
                        wi.data());

@@ -59,3 +59,25 @@ def test_gpumatmult_argument_checks_need_no_gpu():
     assert call(ok, 2, 2, 2) == N.ERR_CAPACITY       # 5 sources > 2 x 2
     assert call(ok, 2, 2, 3, sigma=0.0) == N.ERR_ARG
     assert L.prbf_gpumatmult_3d(fp, fp, None, fp, fp, fp, fp, fp, ip(ok), 2, 0.1, 2, 3) == N.ERR_ARG
+
+
+def test_entry_points_refuse_bad_arguments_before_any_cuda_call():
+    import numpy as np
+    from petrbf_gb300 import _native as N
+    L = N.lib()
+    d = np.zeros(8)
+    dp = d.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    # a null context is an argument error on every context call
+    assert L.prbf_interpolate(None, 8, dp, dp, None, dp, 1, dp, None) == N.ERR_ARG
+    assert L.prbf_matvec(None, dp, dp) == N.ERR_ARG
+    assert L.prbf_pc_apply(None, dp, dp) == N.ERR_ARG
+    assert L.prbf_batch_interpolate(None, 1, None, None, None, None) == N.ERR_ARG
+    assert L.prbf_ctx_synchronize(None) == N.ERR_ARG
+    # RBFInterpolation (3d/wrapper.cxx:20): no grid points, or a particle field to evaluate
+    # first (xg[0] != xp[0]) with a missing array
+    g = np.arange(4, dtype=np.float32)
+    q = g + 1
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    args = lambda ng, yp: (0, None, ng, fp(g), fp(g), fp(g), fp(g), 4, fp(q), yp, fp(q), fp(q), 0.1, 2, 6, 16)
+    assert L.prbf_RBFInterpolation(*args(0, fp(q))) == N.ERR_ARG
+    assert L.prbf_RBFInterpolation(*args(4, None)) == N.ERR_ARG
