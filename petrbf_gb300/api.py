@@ -23,6 +23,13 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(_D)
 
 
+def _check_len(n, **arrays):
+    """Every array given (None skipped) holds n entries: the C side reads n of each."""
+    for name, a in arrays.items():
+        if a is not None and a.shape[0] != n:
+            raise ValueError(f"{name} holds {a.shape[0]} entries, expected {n}")
+
+
 class Context:
     """One GPU context (device memory + one CUDA stream) with fixed solver parameters."""
 
@@ -76,12 +83,18 @@ class Context:
     # ---- MatShell seam -----------------------------------------------------------
     def matvec_setup(self, x, y, z=None):
         x, y, z = _f64(x), _f64(y), _f64(z)
+        _check_len(x.shape[0], y=y, z=z)
+        if self.dim == 3 and z is None:
+            raise ValueError("a 3D context needs z")
         self.n = x.shape[0]
         self._keep = (x, y, z)
         self._check(N.lib().prbf_matvec_setup(self.h, self.n, _ptr(x), _ptr(y), _ptr(z)))
 
     def matvec(self, v):
         v = _f64(v)
+        if self.n is None:
+            raise PrbfError(N.ERR_STATE, "matvec_setup has not been called")
+        _check_len(self.n, v=v)
         out = np.empty_like(v)
         self._check(N.lib().prbf_matvec(self.h, _ptr(v), _ptr(out)))
         return out
@@ -128,6 +141,9 @@ class Context:
 
     def pc_apply(self, r):
         r = _f64(r)
+        if self.n is None:
+            raise PrbfError(N.ERR_STATE, "matvec_setup has not been called")
+        _check_len(self.n, r=r)
         out = np.empty_like(r)
         self._check(N.lib().prbf_pc_apply(self.h, _ptr(r), _ptr(out)))
         return out
@@ -138,6 +154,9 @@ class Context:
         x, y, z = _f64(x), _f64(y), _f64(z)
         f = np.asarray(f, np.float64)
         n = x.shape[0]
+        _check_len(n, y=y, z=z, f=f)
+        if self.dim == 3 and z is None:
+            raise ValueError("a 3D context needs z")
         nrhs = 1 if f.ndim == 1 else f.shape[1]
         fr = np.ascontiguousarray(f.T if f.ndim == 2 else f)
         g = np.empty_like(fr)
@@ -152,6 +171,10 @@ class Context:
 
     def evaluate(self, xt, yt, zt, xs, ys, zs, gs):
         xt, yt, zt, xs, ys, zs, gs = map(_f64, (xt, yt, zt, xs, ys, zs, gs))
+        _check_len(xt.shape[0], yt=yt, zt=zt)
+        _check_len(xs.shape[0], ys=ys, zs=zs, gs=gs)
+        if self.dim == 3 and (zt is None or zs is None):
+            raise ValueError("a 3D context needs z coordinates")
         w = np.empty(xt.shape[0], np.float64)
         self._check(N.lib().prbf_evaluate(self.h, xt.shape[0], _ptr(xt), _ptr(yt), _ptr(zt), xs.shape[0],
                                            _ptr(xs), _ptr(ys), _ptr(zs), _ptr(gs), _ptr(w)))
@@ -167,6 +190,9 @@ def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="
     keep, probs, outs = [], [], []
     for q in problems:
         arrs = [_f64(q[k]) for k in ("x", "y")] + [_f64(q.get("z")), _f64(q["f"])]
+        _check_len(arrs[0].shape[0], y=arrs[1], z=arrs[2], f=arrs[3])
+        if dim == 3 and arrs[2] is None:
+            raise ValueError("3D problems need z")
         g = np.empty(arrs[0].shape[0], np.float64)
         keep.append(arrs)
         outs.append(g)
@@ -231,6 +257,8 @@ def RBFInterpolation(xg, yg, zg, wg, xp, yp, zp, gp, sigma, nsigma_box, sigma_bu
         raise TypeError("wg must be a contiguous float32 array (it is overwritten)")
     fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     xg_, yg_, zg_, xp_, yp_, zp_, gp_ = arrs
+    _check_len(len(xg_), yg=yg_, zg=zg_, wg=wg)
+    _check_len(len(xp_), yp=yp_, zp=zp_, gp=gp_)
     return N.lib().prbf_RBFInterpolation(0, None, len(xg_), fp(xg_), fp(yg_), fp(zg_), fp(wg),
                                          len(xp_), fp(xp_), fp(yp_), fp(zp_), fp(gp_),
                                          float(sigma), int(nsigma_box), int(sigma_buffer),
@@ -249,6 +277,10 @@ def gpumatmult(tx, ty, tz, sx, sy, sz, sg, offset, sigma, num_cluster=None, num_
     iblok = len(off) - 1
     if iblok < 0 or len(tx) != 128 * iblok:
         raise ValueError("targets must hold 128 slots per block and offset iblok + 1 entries")
+    _check_len(len(tx), ty=ty, tz=tz)
+    for name, a in (("sx", sx), ("sy", sy), ("sz", sz), ("sg", sg)):
+        if a is not None and iblok > 0 and len(a) < int(off[-1]):
+            raise ValueError(f"{name} holds {len(a)} entries, fewer than offset[-1] = {int(off[-1])}")
     ncl = iblok if num_cluster is None else int(num_cluster)
     ntr = (max(1, -(-int(off[-1]) // max(ncl, 1))) if iblok else 0) if num_trunc is None else int(num_trunc)
     tw = np.zeros(128 * iblok, np.float32)

@@ -81,3 +81,19 @@ def test_entry_points_refuse_bad_arguments_before_any_cuda_call():
     args = lambda ng, yp: (0, None, ng, fp(g), fp(g), fp(g), fp(g), 4, fp(q), yp, fp(q), fp(q), 0.1, 2, 6, 16)
     assert L.prbf_RBFInterpolation(*args(0, fp(q))) == N.ERR_ARG
     assert L.prbf_RBFInterpolation(*args(4, None)) == N.ERR_ARG
+
+
+def test_python_mirror_checks_array_lengths_before_any_cuda_call():
+    import numpy as np
+    import pytest
+    from petrbf_gb300.api import RBFInterpolation, batch_interpolate, gpumatmult
+    a4, a3 = np.zeros(4), np.zeros(3)
+    with pytest.raises(ValueError):
+        batch_interpolate([dict(x=a4, y=a3, f=a4, sigma=0.1, nsigma_box=4, sigma_buffer=12, sigma_trunc=20)])
+    with pytest.raises(ValueError):
+        RBFInterpolation(a4, a4, a4, np.zeros(4, np.float32), a4, a3, a4, a4, 0.1, 2, 6, 16)
+    t = np.zeros(128)
+    with pytest.raises(ValueError):   # sources shorter than offset[-1]
+        gpumatmult(t, t, None, a3, a3, None, a3, [0, 4], 0.1)
+    with pytest.raises(ValueError):   # targets of different lengths
+        gpumatmult(t, np.zeros(127), None, a4, a4, None, a4, [0, 4], 0.1)
