@@ -33,6 +33,21 @@ def _dp(a):
     return None if a is None else a.ctypes.data_as(_D)
 
 
+def _check_shapes(X, T=None, M=None):
+    """X holds rows of IN features, T and M rows of OUT values, one per row of X."""
+    if X.ndim != 2 or X.shape[1] != IN:
+        raise ValueError(f"features must be [n, {IN}], got {X.shape}")
+    for name, a in (("T", T), ("M", M)):
+        if a is not None and a.shape != (X.shape[0], OUT):
+            raise ValueError(f"{name} must be [{X.shape[0]}, {OUT}], got {a.shape}")
+
+
+def _check_points(x, *arrays):
+    for a in arrays:
+        if a is not None and a.shape[0] != x.shape[0]:
+            raise ValueError(f"arrays of {a.shape[0]} and {x.shape[0]} points")
+
+
 def param_count():
     return int(N.lib().prbf_mlp_param_count())
 
@@ -67,17 +82,20 @@ class Network:
     @weights.setter
     def weights(self, w):
         w = np.ascontiguousarray(w, np.float32)
-        assert w.size == param_count()
+        if w.size != param_count():
+            raise ValueError(f"{w.size} weights, the network has {param_count()}")
         self._chk(N.lib().prbf_mlp_set_weights(self.h, _fp(w)), "set_weights")
 
     def forward(self, X):
         X = np.ascontiguousarray(X, np.float32)
+        _check_shapes(X)
         Y = np.empty((X.shape[0], OUT), np.float32)
         self._chk(N.lib().prbf_mlp_forward(self.h, X.shape[0], _fp(X), _fp(Y)), "forward")
         return Y
 
     def loss_grad(self, X, T, M):
         X, T, M = (np.ascontiguousarray(a, np.float32) for a in (X, T, M))
+        _check_shapes(X, T, M)
         g = np.empty(param_count(), np.float32)
         loss = ctypes.c_float(0)
         self._chk(N.lib().prbf_mlp_loss_grad(self.h, X.shape[0], _fp(X), _fp(T), _fp(M),
@@ -86,6 +104,7 @@ class Network:
 
     def train(self, X, T, M, epochs=40, batch=512, lr=1e-3, seed=1):
         X, T, M = (np.ascontiguousarray(a, np.float32) for a in (X, T, M))
+        _check_shapes(X, T, M)
         hist = np.zeros(max(epochs, 1), np.float32)
         self._chk(N.lib().prbf_mlp_train(self.h, X.shape[0], _fp(X), _fp(T), _fp(M), int(epochs),
                                          int(batch), float(lr), int(seed), _fp(hist)), "train")
@@ -96,6 +115,7 @@ def patches(ctx, x, y, f, g=None):
     """Features X [npatch, 256], per-patch output scale and (with g) targets T and masks M."""
     x, y, f = (np.ascontiguousarray(a, np.float64) for a in (x, y, f))
     g = None if g is None else np.ascontiguousarray(g, np.float64)
+    _check_points(x, y, f, g)
     L = N.lib()
     npatch = ctypes.c_int(0)
     ctx._check(L.prbf_guess_patches(ctx.h, len(x), _dp(x), _dp(y), _dp(f), _dp(g), None, None, None,
@@ -161,11 +181,14 @@ def load(path=MODEL_PATH):
 def install(ctx, weights=None):
     """Puts the trained weights in a Context so PRBF_GUESS_LEARNED solves can use them."""
     w = load() if weights is None else np.ascontiguousarray(weights, np.float32)
+    if w.size != param_count():
+        raise ValueError(f"{w.size} weights, the network has {param_count()}")
     ctx._check(N.lib().prbf_guess_set_weights(ctx.h, _fp(w)))
 
 
 def guess(ctx, x, y, f):
     x, y, f = (np.ascontiguousarray(a, np.float64) for a in (x, y, f))
+    _check_points(x, y, f)
     g0 = np.empty_like(x)
     ctx._check(N.lib().prbf_guess_eval(ctx.h, len(x), _dp(x), _dp(y), _dp(f), _dp(g0)))
     return g0
