@@ -152,6 +152,14 @@ def matvec(g, xs, ys, zs, cs, v):
     return gauss_sum(g, xs, ys, zs, cs, xs, ys, zs, v, cs)
 
 
+def buffer_counts(g, xs, ys, zs, cs):
+    """Points of every cell's Schwarz block (2d/get_buffer.h:9-90), without the lists."""
+    cnt = np.empty(g.ncell, np.int32)
+    lib().orc_buffer_counts(ctypes.byref(g), _d(_f64(xs)), _d(_f64(ys)), _d(_f64(zs)),
+                            _i(cs), _i(cnt))
+    return cnt
+
+
 def buffer_lists(g, xs, ys, zs, cs):
     cnt = np.empty(g.ncell, np.int32)
     lib().orc_buffer_counts(ctypes.byref(g), _d(_f64(xs)), _d(_f64(ys)), _d(_f64(zs)),
