@@ -340,16 +340,17 @@ def run_ours(args, rank, world):
 
 
 def cpu_solve_section(p2, dev, pairs2, gpu2):
-    """The solve on the host cores beside the GPU: config 1 (10^4-point lattice) solved to
-    1e-13 by the oracle (the C++ restatement of the reference's solve: cell list, dense
+    """The solve on the host cores beside the GPU: the 10^4-point 100 x 100 lattice solved
+    to 1e-13 by the oracle (the C++ restatement of the reference's solve: cell list, dense
     Schwarz blocks, GMRES(30); OpenMP over cells) and by the plain FP64 GPU form, and the
-    oracle's time for config 2 extrapolated from config 1's rates: block set-up by the sum
-    of n_b^3, Schwarz applies by the sum of n_b^2, matvecs by the pairs, with config 2's
-    GPU iteration count (a full config-2 CPU solve takes far longer than a bench run)."""
+    oracle's time for the 4x10^6-point problem p2 extrapolated from the small solve's rates:
+    block set-up by the sum of n_b^3, Schwarz applies by the sum of n_b^2, matvecs by the
+    pairs, with p2's GPU iteration count (a full CPU solve of p2 takes far longer than a
+    bench run)."""
     import oracle as O
     from petrbf_gb300 import workloads as W
     from petrbf_gb300.api import Context
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     prm = p.params()
     with Context(dim=2, sigma=p.sigma, nsigma_box=prm[1], sigma_buffer=prm[2], sigma_trunc=prm[3],
                  device=dev) as c:
@@ -380,7 +381,7 @@ def cpu_solve_section(p2, dev, pairs2, gpu2):
     R.close()
     pairs1 = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
     nb1 = O.buffer_counts(g, xs, ys, None, cs).astype(np.float64)
-    # config 2's blocks, from its own cell list
+    # p2's blocks, from its own cell list
     g2 = O.grid_for(p2.x, p2.y, None, *p2.params())
     perm2, cs2 = O.cell_sort(g2, p2.x, p2.y)
     nb2 = O.buffer_counts(g2, p2.x[perm2], p2.y[perm2], None, cs2).astype(np.float64)
@@ -392,7 +393,7 @@ def cpu_solve_section(p2, dev, pairs2, gpu2):
     rel = float(np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu))
     return {
         "cores": O.num_threads(), "kind": "port",
-        "config1": {"workload": p.name, "n_points": p.n,
+        "lamb_oseen_lattice_1e4": {"workload": p.name, "n_points": p.n,
                     "cpu_time_s": t3 - t0, "cpu_setup_s": t2 - t1, "cpu_gmres_s": t3 - t2, "cpu_its": its,
                     "cpu_reason": reason, "gpu_time_s": gpu_s, "gpu_its": st.its,
                     "weights_rel_diff_gpu_vs_cpu": rel,
@@ -400,10 +401,10 @@ def cpu_solve_section(p2, dev, pairs2, gpu2):
                                     "settle; solved to rtol 1e-16 they agree within 1e-10 (tests)",
                     "cpu_pts_per_s": p.n / (t3 - t0),
                     "gpu_pts_per_s": p.n / gpu_s},
-        "config2_extrapolated": {"cpu_time_s": cpu2, "cpu_setup_s": setup2, "cpu_iterations_s": iter2,
+        "lamb_oseen_jitter_4e6_extrapolated": {"cpu_time_s": cpu2, "cpu_setup_s": setup2, "cpu_iterations_s": iter2,
                                  "its": its2, "block_flops_ratio": r3, "gpu_fp64_time_s": gpu2["time_s"],
                                  "cpu_pts_per_s": p2.n / cpu2,
-                                 "basis": "config-1 rates scaled by sum n_b^3 (set-up), sum n_b^2 (applies), "
+                                 "basis": "the 10^4-point solve's rates scaled by sum n_b^3 (set-up), sum n_b^2 (applies), "
                                           "pairs (matvecs); its + 1 applies and matvecs"},
     }
 
@@ -450,7 +451,7 @@ def run_vortex3d(args, rank):
     plain FP64 GPU solve of the same problem (the form the tests pin to the oracle)."""
     from petrbf_gb300 import workloads as W
     from petrbf_gb300.api import Context
-    p = W.config3(m=args.m3)
+    p = W.vortex_ring_3d(m=args.m3)
     nb, sb, st_ = p.nsigma_box, p.sigma_buffer, p.sigma_trunc
     out = {}
     sols = {}
@@ -490,7 +491,7 @@ def run_batch2d(args, rank):
     from petrbf_gb300.api import batch_interpolate
     peak = fp64_peak_tflops(torch)
     out = {}
-    for kind, probs in (("scattered", W.config4(nprob=args.nprob)), ("lattice", W.config4_lattice(nprob=args.nprob))):
+    for kind, probs in (("scattered", W.batch_scattered(nprob=args.nprob)), ("lattice", W.batch_lattice(nprob=args.nprob))):
         for prec in ("fp64", "mixed"):
             res = {}
             for rep in range(2):  # second call: schedule from the autotuner's cache
@@ -546,7 +547,7 @@ def run_case(name):
     import torch
     from petrbf_gb300 import workloads as W
     from petrbf_gb300.api import Context, batch_interpolate
-    if name in ("gauss32_2d", "gauss64_2d"):  # 10^6-point jittered lattice, config-2 geometry
+    if name in ("gauss32_2d", "gauss64_2d"):  # 10^6-point jittered lattice, 8-sigma-cell geometry
         x, y, h = W.lattice_2d(1000, jitter=0.25, seed=1)
         c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
         c.matvec_setup(x, y)
@@ -556,7 +557,7 @@ def run_case(name):
         for _ in range(3):
             c.matvec_dev(v.data_ptr(), o.data_ptr(), cell_order=True, fp32=(name == "gauss32_2d"))
         c.synchronize()
-    elif name in ("gauss32_3d", "gauss64_3d"):  # 48^3 jittered lattice, config-3 geometry
+    elif name in ("gauss32_3d", "gauss64_3d"):  # 48^3 jittered lattice, 3D vortex-ring geometry
         x, y, z, h = W.lattice_3d(48, jitter=0.25, seed=1)
         c = Context(dim=3, sigma=h / 0.8, nsigma_box=3, sigma_buffer=7, sigma_trunc=17)
         c.matvec_setup(x, y, z)
@@ -574,7 +575,7 @@ def run_case(name):
         r = np.random.default_rng(1).standard_normal(len(x))
         for _ in range(3):
             c.pc_apply(r)
-    elif name == "chol64_2d":  # FP64 block factorisation, 400^2 jittered lattice, config-2 blocks
+    elif name == "chol64_2d":  # FP64 block factorisation, 400^2 jittered lattice, 8-sigma-cell blocks
         x, y, h = W.lattice_2d(400, jitter=0.25, seed=1)
         c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
         c.matvec_setup(x, y)
@@ -582,7 +583,7 @@ def run_case(name):
         r = np.random.default_rng(1).standard_normal(len(x))
         for _ in range(3):
             c.pc_apply(r)
-    elif name == "chol32_2d":  # FP32 restricted blocks (S_c form), 400^2 jittered lattice, config-2 blocks
+    elif name == "chol32_2d":  # FP32 restricted blocks (S_c form), 400^2 jittered lattice, 8-sigma-cell blocks
         x, y, h = W.lattice_2d(400, jitter=0.25, seed=1)
         c = Context(dim=2, sigma=h / 0.8, nsigma_box=8, sigma_buffer=24, sigma_trunc=24)
         c.matvec_setup(x, y)
@@ -591,9 +592,9 @@ def run_case(name):
         for _ in range(3):
             c.pc_apply(r)
     elif name == "batch":  # 24 problems of the batched form (N up to 6x10^4)
-        batch_interpolate(W.config4(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
+        batch_interpolate(W.batch_scattered(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
     elif name == "batch_mixed":  # 24 jittered-lattice problems of the batched form, mixed
-        batch_interpolate(W.config4_lattice(nprob=24, nmax=60000), rtol=1e-13, pc="asm", precision="mixed")
+        batch_interpolate(W.batch_lattice(nprob=24, nmax=60000), rtol=1e-13, pc="asm", precision="mixed")
     elif name == "seam_2d":  # the gpumatmult seam on the packed arrays of a 10^6-point lattice
         run_seam_case()
         return

@@ -103,17 +103,17 @@ def lamb_oseen_2d(m, jitter=0.0, seed=12345, overlap=0.8, nsigma_box=8, name=Non
                    meta={"m": m, "h": h, "jitter": jitter, "seed": seed, "overlap": overlap})
 
 
-def config1():
+def lamb_oseen_lattice_1e4():
     """2D plain FP64, N = 10^4 on a 100x100 lattice over [-1,1]^2 (h = 0.02)."""
     return lamb_oseen_2d(100, name="2d_lamb_oseen_N1e4_lattice")
 
 
-def config2(m=2000, seed=12345):
+def lamb_oseen_jitter_4e6(m=2000, seed=12345):
     """2D plain FP64 at scale: N = 4x10^6 on a 2000x2000 lattice, +/-0.25h seeded jitter."""
     return lamb_oseen_2d(m, jitter=0.25, seed=seed, name="2d_lamb_oseen_N4e6_jitter")
 
 
-def config3(m=128, seed=12345, nsigma_box=3, sigma_buffer=7):
+def vortex_ring_3d(m=128, seed=12345, nsigma_box=3, sigma_buffer=7):
     """3D vortex ring, N = 128^3 jittered lattice, three right-hand sides; cutoff 7 sigma
     past the cell edge (sigma_trunc = nsigma_box + 14). Cell 3 sigma (~53 points) and a
     7-sigma Schwarz box (2 sigma of overlap on each side, blocks of up to 729 points): on
@@ -129,7 +129,7 @@ def config3(m=128, seed=12345, nsigma_box=3, sigma_buffer=7):
                    meta={"m": m, "h": h, "jitter": 0.25, "seed": seed})
 
 
-def config4(nprob=256, seed=2024, nmin=2000, nmax=200000, nsigma_box=4):
+def batch_scattered(nprob=256, seed=2024, nmin=2000, nmax=200000, nsigma_box=4):
     """Batched 2D: nprob independent problems, N log-uniform in [nmin, nmax], points
     uniform-random in [-1,1]^2, h = 2/sqrt(N), h/sigma uniform in [0.6, 1.0], Lamb-Oseen
     right-hand side (G = 1, t = 1) with centre uniform in [-0.5,0.5]^2 and core radius
@@ -177,10 +177,10 @@ def cylinder_problem(x, y, e, overlap=0.9, nsigma_box=5, buffer_factor=1.9):
                    exact=e, meta={"overlap": overlap})
 
 
-def config4_lattice(nprob=256, seed=2025, nmin=2000, nmax=200000, nsigma_box=4):
-    """The lattice counterpart of config4: the same N distribution, each problem an m x m
+def batch_lattice(nprob=256, seed=2025, nmin=2000, nmax=200000, nsigma_box=4):
+    """The lattice counterpart of batch_scattered: the same N distribution, each problem an m x m
     lattice (m = round(sqrt(N))) over [-1,1]^2 with +/-0.25h seeded jitter, h = 2/m, h/sigma
-    uniform in [0.6, 1.0], Lamb-Oseen right-hand side as in config4."""
+    uniform in [0.6, 1.0], Lamb-Oseen right-hand side as in batch_scattered."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(nprob):
@@ -199,7 +199,7 @@ def config4_lattice(nprob=256, seed=2025, nmin=2000, nmax=200000, nsigma_box=4):
 
 def pack_gpumatmult_2d(m=1000, seed=1):
     """Packs a jittered m x m lattice the way the reference's host packer does
-    (2d/matmultgpu.cxx:39-71) for the config-2 geometry (cell 8 sigma, sources of a cell =
+    (2d/matmultgpu.cxx:39-71) for the 8-sigma-cell geometry (cell 8 sigma, sources of a cell =
     the points of its 3 x 3 cells, which the 12 sigma truncation box spans): 128 FP32
     target slots per cell, the cells' source sets one after the other, CSR offsets."""
     x, y, h = lattice_2d(m, jitter=0.25, seed=seed)

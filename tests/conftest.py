@@ -19,7 +19,7 @@ def load_golden(name):
     d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
     if "x" not in d:  # lattice fixtures store no inputs: regenerate them exactly
         from petrbf_gb300 import workloads as W
-        p = W.config1()
+        p = W.lamb_oseen_lattice_1e4()
         d["x"], d["y"] = p.x, p.y
     return d
 

@@ -75,7 +75,7 @@ def main(ref_root):
         if not O.ref_available(d, ref_root):
             raise SystemExit("reference %dd tree not found under %s" % (d, ref_root))
     # 1. the 2D lattice case of the headline workload: N=10^4, h=0.02, sigma=h/0.8
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     xs = -1.0 + np.arange(199) * 0.01  # main2-style half-spacing evaluation grid
     xt, yt = np.repeat(xs, 199), np.tile(xs, 199)
     _case("g2d_lattice100", 2, p.x, p.y, None, *p.params(), blocks=(0, 45, 99),

@@ -15,7 +15,7 @@ def _rel(a, b):
 
 
 def _small_batch(k=10, seed=7):
-    return W.config4(nprob=k, seed=seed, nmin=500, nmax=6000)
+    return W.batch_scattered(nprob=k, seed=seed, nmin=500, nmax=6000)
 
 
 def _true_resid(q, g):
@@ -75,7 +75,7 @@ def test_mixed_batch_meets_the_fp64_residual_and_routes_ill_conditioned_problems
     # h/sigma >= 0.72 are well enough conditioned for it; uniform-random points (pairs far
     # closer than h) and the lattice with h/sigma 0.64 have blocks whose FP32 Cholesky fails
     # (smallest eigenvalues 1e-7 .. 5e-11), and are solved as an FP64 batch instead
-    lat = W.config4_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
+    lat = W.batch_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
     probs = lat + _small_batch(3, seed=5)
     g, its, reason, st = batch_interpolate(probs, rtol=1e-13, pc="asm", precision="mixed")
     assert st.nconverged == len(probs) and all(r > 0 for r in reason)

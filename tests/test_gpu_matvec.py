@@ -94,7 +94,7 @@ def test_evaluation_matches_reference(golden, case):
 
 
 def test_matvec_medium_jittered_vs_oracle():
-    p = W.lamb_oseen_2d(400, jitter=0.25, seed=11)  # 160k points, config-2 geometry
+    p = W.lamb_oseen_2d(400, jitter=0.25, seed=11)  # 160k points, 8-sigma-cell geometry
     rng = np.random.default_rng(0)
     v = rng.standard_normal(p.n)
     with Context(dim=2, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
@@ -164,7 +164,7 @@ def test_bounded_wait_timeout_is_reported_and_the_context_survives():
         assert abs(y[0] - 2.0 / (2 * np.pi * 0.01)) < 1e-12 * y[0]
 
 
-@pytest.mark.parametrize("which", ["config2", "config3"])
+@pytest.mark.parametrize("which", ["lamb_oseen_jitter_4e6", "vortex_ring_3d"])
 def test_full_size_matvec_rows_against_oracle(which):
     # the full-size workloads (4x10^6 points in 2D, 128^3 in 3D): 2000 sampled rows of the
     # GPU's FP64 sum against the oracle's evaluation of the same sum at those points, and
@@ -193,10 +193,10 @@ def test_full_size_matvec_rows_against_oracle(which):
 
 
 def test_symmetric_form_where_it_applies():
-    # 2D config-1 geometry (5 x 5 window: 12 upper cells): the FP64 product takes the
+    # The 10^4-point lattice (5 x 5 window: 12 upper cells): the FP64 product takes the
     # symmetric form (sum + gather); a 3D 7 x 7 x 7 window (171 upper cells) keeps the
     # one-sided kernel; FP32 products are the conversion and the sum
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     with Context(dim=2, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
                  sigma_trunc=p.sigma_trunc) as c:
         c.matvec_setup(p.x, p.y)

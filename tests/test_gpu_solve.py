@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 RTOL_WEIGHTS = 1e-10
 # At the reference's stopping rule (rtol 1e-13 on the preconditioned residual) GMRES
 # stops before the weights settle: the oracle's own 1e-13 solution differs from its
-# converged one by 1.5e-10 on config 1, so two implementations agree to a few 1e-10.
+# converged one by 1.5e-10 on the 10^4-point lattice, so two implementations agree to a few 1e-10.
 RTOL_WEIGHTS_AT_1E13 = 5e-10
 
 
@@ -60,8 +60,8 @@ def test_rasm_apply_matches_oracle(jitter):
     assert _rel(z32, ref) < 0.2  # FP32 factors: a preconditioner, not a solve
 
 
-def test_solve_config1_fp64_converged_weights_match_oracle():
-    p = W.config1()
+def test_solve_lamb_oseen_lattice_1e4_fp64_converged_weights_match_oracle():
+    p = W.lamb_oseen_lattice_1e4()
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), rtol=1e-16,
                                               max_it=300)
     with _ctx(p, rtol=1e-16, max_it=300) as c:
@@ -78,7 +78,7 @@ def test_solve_config1_fp64_converged_weights_match_oracle():
 def test_true_residual_solve_matches_oracle_converged():
     """The mixed form stops on the true FP64 residual: at rtol 1e-15 it reaches the
     discrete solution, whose interpolation error must match the oracle's converged one."""
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), rtol=1e-16,
                                               max_it=300)
     with _ctx(p, precision="mixed", rtol=1e-15) as c:
@@ -88,8 +88,8 @@ def test_true_residual_solve_matches_oracle_converged():
     assert abs(_offgrid_err(p, g) - _offgrid_err(p, go)) < 1e-3
 
 
-def test_solve_config1_fp64_matches_oracle():
-    p = W.config1()
+def test_solve_lamb_oseen_lattice_1e4_fp64_matches_oracle():
+    p = W.lamb_oseen_lattice_1e4()
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params())
     with _ctx(p) as c:
         g, st = c.interpolate(p.x, p.y, None, p.f)
@@ -109,7 +109,7 @@ def test_solve_config1_fp64_matches_oracle():
 def test_interpolation_error_matches_oracle_narrow_core(precision):
     """Narrow Lamb-Oseen core (nu = 0.001): the interpolation error (10^-8.8) dominates
     the solver's, so the reference's error metric must come out the same."""
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     f = W.lamb_oseen(p.x, p.y, nu=0.001)
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, f, *p.params())
     with _ctx(p, precision=precision) as c:
@@ -119,8 +119,8 @@ def test_interpolation_error_matches_oracle_narrow_core(precision):
     assert e < -8 and abs(e - eo) < 1e-3
 
 
-def test_solve_config1_mixed_reaches_fp64_answer():
-    p = W.config1()
+def test_solve_lamb_oseen_lattice_1e4_mixed_reaches_fp64_answer():
+    p = W.lamb_oseen_lattice_1e4()
     with _ctx(p) as c:
         g64, st64 = c.interpolate(p.x, p.y, None, p.f)
     with _ctx(p, precision="mixed") as c:
@@ -135,7 +135,7 @@ def test_mixed_falls_back_to_fp64_on_ill_conditioned_points():
     # uniform-random points: blocks with smallest eigenvalues near 5e-11 (far below FP32's
     # resolution); the refinement stalls and the call is solved in FP64, to the plain
     # form's answer. A jittered lattice at h/sigma 0.97 stays in the mixed form.
-    q = W.config4(nprob=1, seed=5, nmin=3000, nmax=4000)[0]
+    q = W.batch_scattered(nprob=1, seed=5, nmin=3000, nmax=4000)[0]
     args = (q["sigma"], q["nsigma_box"], q["sigma_buffer"], q["sigma_trunc"])
     kw = dict(sigma=q["sigma"], nsigma_box=q["nsigma_box"], sigma_buffer=q["sigma_buffer"],
               sigma_trunc=q["sigma_trunc"], pc="asm")
@@ -150,7 +150,7 @@ def test_mixed_falls_back_to_fp64_on_ill_conditioned_points():
     perm, cs = O.cell_sort(gr, q["x"], q["y"])
     r = O.matvec(gr, q["x"][perm], q["y"][perm], None, cs, gm[perm]) - q["f"][perm]
     assert np.linalg.norm(r) / np.linalg.norm(q["f"]) < 1e-10
-    lat = [p for p in W.config4_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
+    lat = [p for p in W.batch_lattice(nprob=6, seed=9, nmin=500, nmax=6000)
            if p["meta"]["h_over_sigma"] > 0.95][0]
     with Context(precision="mixed", sigma=lat["sigma"], nsigma_box=lat["nsigma_box"],
                  sigma_buffer=lat["sigma_buffer"], sigma_trunc=lat["sigma_trunc"], pc="asm") as c:
@@ -296,7 +296,7 @@ def test_rbfinterpolation_shim_matches_evaluate_then_solve():
 
 
 def test_solve_errors():
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     with _ctx(p, max_it=2) as c:
         with pytest.raises(PrbfError) as e:
             c.interpolate(p.x, p.y, None, p.f)
@@ -339,7 +339,7 @@ def test_edge_point_sets(precision):
     # collisions: five points repeated with the same value -- singular blocks (the reference's
     # PETSc LU stops on the zero pivot); the blocks are factored with a diagonal shift and the
     # consistent system is still solved to the tolerance (the mixed form hands it to FP64)
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     idx = np.arange(10, 15)
     x, y = np.concatenate([p.x, p.x[idx]]), np.concatenate([p.y, p.y[idx]])
     f = np.concatenate([p.f, p.f[idx]])

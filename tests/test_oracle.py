@@ -161,8 +161,8 @@ def test_gmres_solves_small_system_to_tolerance():
     assert hist[-1] <= 1e-13 * hist[0]
 
 
-def test_rbf_interpolation_config1_error():
-    p = W.config1()
+def test_rbf_interpolation_lamb_oseen_lattice_1e4_error():
+    p = W.lamb_oseen_lattice_1e4()
     gw, its, reason = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params())
     assert reason == 2 and 5 <= its <= 40
     w = O.vorticity_evaluation(p.x, p.y, None, p.x, p.y, None, gw, *p.params())

@@ -20,7 +20,7 @@ MAX_POINTS = 1048576  # PRBF_STATIC_SORT_MAX_POINTS
 def _cases():
     x3, y3, z3, h3 = W.lattice_3d(40, jitter=0.25, seed=9)
     return [
-        (2, W.config1().x, W.config1().y, None, (0.025, 8, 24, 24)),
+        (2, W.lamb_oseen_lattice_1e4().x, W.lamb_oseen_lattice_1e4().y, None, (0.025, 8, 24, 24)),
         (2, *W.lattice_2d(1000, jitter=0.25, seed=3)[:2], None, (1.25e-3 * 2, 8, 24, 24)),
         (3, x3, y3, z3, (h3 / 0.8, 2, 10, 16)),
     ]
@@ -67,7 +67,7 @@ def test_static_sort_rejects_sizes_beyond_its_limits():
                                  24, 24, ibuf.data_ptr(), ibuf.data_ptr(), 4, ctypes.byref(ncell), None)
     assert st == N.ERR_CAPACITY
     # cell_start capacity smaller than ncell + 1
-    p = W.config1()
+    p = W.lamb_oseen_lattice_1e4()
     xd = torch.tensor(p.x, device="cuda")
     yd = torch.tensor(p.y, device="cuda")
     perm = torch.empty(p.n, dtype=torch.int32, device="cuda")
