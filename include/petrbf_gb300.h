@@ -26,7 +26,8 @@ enum {
   PRBF_OK = 0,
   PRBF_ERR_ARG = 1,           /* bad argument (null pointer, n <= 0, dim not 2/3, ...) */
   PRBF_ERR_RANGE = 2,         /* parameters or coordinates outside the supported range */
-  PRBF_ERR_CAPACITY = 3,      /* a size exceeds a kernel or scratch capacity */
+  PRBF_ERR_CAPACITY = 3,      /* a size exceeds a kernel or scratch capacity, or a host
+                               allocation failed */
   PRBF_ERR_CUDA = 4,          /* CUDA runtime error (message in prbf_last_error) */
   PRBF_ERR_NOT_CONVERGED = 5, /* iteration limit reached (KSP_DIVERGED_ITS) */
   PRBF_ERR_BREAKDOWN = 6,     /* GMRES breakdown (KSP_DIVERGED_BREAKDOWN) */
@@ -207,13 +208,17 @@ typedef struct {
 
 /* Solves every problem with GMRES + Schwarz blocks in one set of launches per iteration
  * (rbf_interpolation per problem, 2d/rbf_interpolation.cxx:25-310); its_out / reason_out
- * (nullable) receive each problem's iterations and KSPConvergedReason-style code. */
+ * (nullable) receive each problem's iterations and KSPConvergedReason-style code. When a
+ * problem stops short of the tolerance the call returns its status (the first failure in
+ * problem order) with every problem's weights, iterations and reason written. */
 int prbf_batch_interpolate(prbf_ctx* ctx, int nprob, const prbf_problem* probs, int* its_out, int* reason_out,
                            prbf_batch_stats* stats);
 
 /* RBFInterpolation (3d/wrapper.cxx:20-105): FP32 in/out, evaluates the particles
  * (xp, yp, zp, gp) at the grid points first when xg[0] != xp[0], then solves on the
- * grid and writes the weights over wg. argc/argv are accepted and ignored. */
+ * grid and writes the weights over wg. argc/argv are accepted and ignored. Arguments are
+ * checked before any CUDA call: ng <= 0, a null grid array, or a particle array missing
+ * when the particles are to be evaluated return PRBF_ERR_ARG. */
 int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, float* zg,
                           float* wg, int np, float* xp, float* yp, float* zp, float* gp,
                           float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc);
