@@ -212,6 +212,8 @@ def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="
         if code:
             err = PrbfError(code, N.lib().prbf_last_error(c.h).decode())
             err.stats = st
+            if code in (N.ERR_NOT_CONVERGED, N.ERR_BREAKDOWN, N.ERR_NAN, N.ERR_DIVERGED):
+                err.results = (outs, its, reason)  # every problem's weights and stop reason
             raise err
     return outs, its, reason, st
 
