@@ -26,6 +26,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "krylov.h"
@@ -75,6 +76,27 @@ struct BatchOp : Operator {
   }
 };
 
+// A pair of timing events, destroyed on every path out (errors throw).
+struct EventPair {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  EventPair() {
+    PRBF_CUDA(cudaEventCreate(&e0));
+    PRBF_CUDA(cudaEventCreate(&e1));
+  }
+  ~EventPair() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+  EventPair(const EventPair&) = delete;
+  EventPair& operator=(const EventPair&) = delete;
+  float ms() const {
+    PRBF_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    PRBF_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    return t;
+  }
+};
+
 struct Schedule {
   int tile = 128;
   int grid = 0;  // CTAs (0: one per item)
@@ -106,6 +128,10 @@ namespace {
 // problems, points), kept for the life of the process.
 std::map<std::pair<int, long long>, Schedule>& schedule_cache() {
   static std::map<std::pair<int, long long>, Schedule> m;
+  return m;
+}
+std::mutex& schedule_mutex() {  // contexts on several host threads share the cache
+  static std::mutex m;
   return m;
 }
 }  // namespace
@@ -153,9 +179,7 @@ Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout, bool f
   const int grids[3] = {0, 152 * 3, 152 * 6};
   Schedule best;
   best.ms = 1e300;
-  cudaEvent_t e0, e1;
-  PRBF_CUDA(cudaEventCreate(&e0));
-  PRBF_CUDA(cudaEventCreate(&e1));
+  EventPair ev;
   for (int tile : tiles) {
     std::vector<int2> all = make_items(B, tile, nullptr), sample;
     for (size_t i = 0; i < all.size(); i += 8) sample.push_back(all[i]);
@@ -163,12 +187,10 @@ Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout, bool f
     for (int grid : grids) {
       B.plan.grid = grid;
       gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, fp32, c.err.get(), c.stream);  // warm-up
-      PRBF_CUDA(cudaEventRecord(e0, c.stream));
+      PRBF_CUDA(cudaEventRecord(ev.e0, c.stream));
       for (int k = 0; k < 2; k++) gauss_sum_dev(B.plan, B.op.v, B.op.v, vin, vout, fp32, c.err.get(), c.stream);
-      PRBF_CUDA(cudaEventRecord(e1, c.stream));
-      PRBF_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      PRBF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      PRBF_CUDA(cudaEventRecord(ev.e1, c.stream));
+      const float ms = ev.ms();
       if (ms < best.ms) {
         best.ms = ms;
         best.tile = tile;
@@ -176,8 +198,6 @@ Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout, bool f
       }
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   c.check_device_error("autotune");
   return best;
 }
@@ -350,13 +370,20 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
                                                     ((long long)nprob << 40) ^ (long long)N);
   Schedule sch;
   double t_tune = 0;
-  auto hit = schedule_cache().find(key);
-  if (hit != schedule_cache().end()) {
-    sch = hit->second;
-  } else {
+  bool cached = false;
+  {
+    std::lock_guard<std::mutex> lk(schedule_mutex());
+    auto hit = schedule_cache().find(key);
+    if (hit != schedule_cache().end()) {
+      sch = hit->second;
+      cached = true;
+    }
+  }
+  if (!cached) {
     const double tt0 = now_ms();
     sch = autotune(c, B, B.b.get(), B.tmp.get(), mixed);
     t_tune = now_ms() - tt0;
+    std::lock_guard<std::mutex> lk(schedule_mutex());
     schedule_cache()[key] = sch;
   }
   long long pairs_check = 0;
@@ -368,18 +395,12 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
                        B.hcs, c.stream);
   // one timed Gaussian sum with the chosen schedule, per precision in use (rates reported)
   auto time_sum = [&](bool fp32) {
-    cudaEvent_t e0, e1;
-    PRBF_CUDA(cudaEventCreate(&e0));
-    PRBF_CUDA(cudaEventCreate(&e1));
+    EventPair ev;
     gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), fp32, c.err.get(), c.stream);
-    PRBF_CUDA(cudaEventRecord(e0, c.stream));
+    PRBF_CUDA(cudaEventRecord(ev.e0, c.stream));
     gauss_sum_dev(B.plan, B.op.v, B.op.v, B.b.get(), B.tmp.get(), fp32, c.err.get(), c.stream);
-    PRBF_CUDA(cudaEventRecord(e1, c.stream));
-    PRBF_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    PRBF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    PRBF_CUDA(cudaEventRecord(ev.e1, c.stream));
+    const float ms = ev.ms();
     PRBF_CUDA(cudaMemsetAsync(B.tmp.get(), 0, sizeof(double) * ldv, c.stream));
     return (double)ms;
   };

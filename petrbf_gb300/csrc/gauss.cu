@@ -25,6 +25,7 @@
 // NV weight vectors (several right-hand sides of one point set, NV <= 4) are summed in
 // one pass: each pair's exponential is computed once and multiplies NV weights.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "device.h"
@@ -1368,7 +1369,7 @@ void launch(const GaussPlan& P, const PointsView& t, const PointsView& s, const 
             long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
   size_t sm = smem_bytes<DIM, F32, NV>();
   static_assert(Layout<DIM, F32, NV>::total <= 227 * 1024, "k_gauss shared memory");
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // per device: attribute set (idempotent, thread-safe)
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
@@ -1392,7 +1393,7 @@ void launch_sym_k(const GaussPlan& P, const PointsView& s, const double* gv, dou
                   const int* skip, cudaStream_t st) {
   constexpr size_t sm = LayoutS<DIM, NV>::total;
   static_assert(sm <= 227 * 1024, "k_gauss_sym shared memory");
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // per device: attribute set (idempotent, thread-safe)
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
@@ -1445,7 +1446,7 @@ void launch_f32m(const GaussPlan& P, const PointsView& t, const PointsView& s, c
                  long long vstride, unsigned* err, const int* skip, cudaStream_t st) {
   constexpr size_t sm = LayoutF<DIM, NV>::total;
   static_assert(sm <= 227 * 1024, "k_gauss_f32m shared memory");
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // per device: attribute set (idempotent, thread-safe)
   int dev = 0;
   PRBF_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !attr_set[dev]) {
