@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -29,7 +30,14 @@ struct DevBuf {
     release();
     size_t bytes = count * sizeof(T);
     if (bytes == 0) bytes = 16;
-    PRBF_CUDA(cudaMalloc((void**)&p, bytes));
+    const cudaError_t e = cudaMalloc((void**)&p, bytes);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();  // an allocation failure is not sticky: later launch checks must not see it
+      if (e == cudaErrorMemoryAllocation)
+        throw Error(PRBF_ERR_CAPACITY, "device memory exhausted (" + std::to_string(bytes) + " bytes requested)");
+      throw Error(PRBF_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
     n = count;
     return p;
   }
