@@ -26,8 +26,8 @@ enum {
   PRBF_OK = 0,
   PRBF_ERR_ARG = 1,           /* bad argument (null pointer, n <= 0, dim not 2/3, ...) */
   PRBF_ERR_RANGE = 2,         /* parameters or coordinates outside the supported range */
-  PRBF_ERR_CAPACITY = 3,      /* a size exceeds a kernel or scratch capacity, or a host
-                               allocation failed */
+  PRBF_ERR_CAPACITY = 3,      /* a size exceeds a kernel or scratch capacity, or device or
+                               host memory is exhausted */
   PRBF_ERR_CUDA = 4,          /* CUDA runtime error (message in prbf_last_error) */
   PRBF_ERR_NOT_CONVERGED = 5, /* iteration limit reached (KSP_DIVERGED_ITS) */
   PRBF_ERR_BREAKDOWN = 6,     /* GMRES breakdown (KSP_DIVERGED_BREAKDOWN) */
