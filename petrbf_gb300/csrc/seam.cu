@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <new>
 
 #include "device.h"
 
@@ -200,6 +201,8 @@ int seam(const float* tX, const float* tY, const float* tZ, float* tW, const flo
     return PRBF_OK;
   } catch (const Error& e) {
     return e.status;
+  } catch (const std::bad_alloc&) {
+    return PRBF_ERR_CAPACITY;
   } catch (const std::exception&) {
     return PRBF_ERR_CUDA;
   }
