@@ -1,0 +1,35 @@
+"""bench.py's CPU-side pieces: the reference arm's JSON line (the oracle port on the host
+cores) and the clock-sample summary that flags throttled runs."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "Gaussian matvec Gpairs/s" and d["unit"] == "Gpairs/s"
+    assert d["value"] > 0 and d["steps"] == 1 and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_clock_summary_reports_throttle_reasons():
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.Clocks(0)
+    c.rows = [["2070", "2070", "Not Active", "Not Active", "Not Active", "Not Active"],
+              ["1980", "2070", "Not Active", "Not Active", "Not Active", "Active"],
+              ["2010", "2070", "Active", "Not Active", "Not Active", "Not Active"]]
+    s = c.summary()
+    assert s["sm_mhz"] == 2010.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert bench.Clocks(0).summary()["reasons"] == ["unsampled"]
