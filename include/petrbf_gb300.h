@@ -106,15 +106,25 @@ typedef struct {
 
 typedef struct prbf_ctx prbf_ctx;
 
+/* Defaults: the reference's run options (2d/Makefile:7: -ksp_rtol 1e-13, -ksp_max_it 1000)
+ * with PETSc's GMRES(30), dtol 1e5 and abstol 1e-50, FP64, zero guess, restricted Schwarz,
+ * device 0. */
 void prbf_params_default(prbf_params* p);
+/* Text of a status code (no reference counterpart: the reference reports through CHKERRQ). */
 const char* prbf_status_string(int status);
 
+/* A context holds what rbf_interpolation builds and tears down on every call -- the solver
+ * (KSPCreate, 2d/rbf_interpolation.cxx:210), the shell operators M and P (:190-198) and
+ * their destruction (:296-307) -- kept across calls with its device memory and one stream. */
 int prbf_ctx_create(const prbf_params* p, prbf_ctx** out);
 int prbf_ctx_destroy(prbf_ctx* ctx);
-/* Last error message of this context (valid until the next call on it). */
+/* Last error message of this context (valid until the next call on it; no reference
+ * counterpart: CHKERRQ prints and returns). */
 const char* prbf_last_error(const prbf_ctx* ctx);
-/* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
+/* The context's CUDA stream (a cudaStream_t), for event timing by the caller (no reference
+ * counterpart). */
 void* prbf_ctx_stream(prbf_ctx* ctx);
+/* Waits for the context's stream (no reference counterpart: the reference's calls block). */
 int prbf_ctx_synchronize(prbf_ctx* ctx);
 /* Self-test of the failure path of the kernels' bounded waits (no counterpart in the
  * reference): a one-warp kernel polls, max_polls times (1 .. 2^20), an mbarrier that
@@ -141,7 +151,10 @@ int prbf_evaluate(prbf_ctx* ctx, int nt, const double* xt, const double* yt, con
  * reference's MATOP_MULT callback mymatmult (2d/matmult.cxx:6-51), host vectors in the
  * caller's order. prbf_matvec_dev takes device pointers (PRBF_ORDER_* | PRBF_MATVEC_FP32). */
 int prbf_matvec_setup(prbf_ctx* ctx, int n, const double* x, const double* y, const double* z);
+/* mymatmult (2d/matmult.cxx:6-51; 3d/matmult.cxx:6-52) on host vectors */
 int prbf_matvec(prbf_ctx* ctx, const double* x_in, double* y_out);
+/* mymatmult on device vectors: the GPU path of 2d/matmultgpu.cxx:9-97 without its per-call
+ * packing and copies */
 int prbf_matvec_dev(prbf_ctx* ctx, const double* x_in_dev, double* y_out_dev, int flags);
 /* Cell-list queries after prbf_matvec_setup: sorted position -> caller index, per-cell
  * start offsets (ncell+1 ints), truncation-set sizes (ncell ints), and grid info
@@ -152,8 +165,12 @@ int prbf_matvec_info(prbf_ctx* ctx, int* ints7, double* dbls4, long long* pairs)
  * the reverse contributions added by a second kernel -- else 1; fp32 = 1: the weight
  * conversion and the FP32 sum) and whether the FP64 product is symmetric. */
 int prbf_matvec_kernels(prbf_ctx* ctx, int fp32, int* kernels, int* symmetric);
+/* the cell sort's permutation (Get_cluster::get_cluster, 2d/get_cluster.h:123-130; the
+ * isort of 2d/rbf_interpolation.cxx:124-128) */
 int prbf_get_permutation(prbf_ctx* ctx, int* perm_out);
+/* the per-cell point ranges (ista/iend of CLUSTER, 2d/par.h:71-124) as ncell + 1 starts */
 int prbf_get_cell_start(prbf_ctx* ctx, int* cell_start_out);
+/* the truncation-set size of every cell (Get_trunc::get_trunc, 2d/get_trunc.h:9-87) */
 int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
 
 /* RASM preconditioner of the points given to prbf_matvec_setup: the reference's P shell
@@ -163,6 +180,7 @@ int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
  * FP64, PRBF_PREC_MIXED in FP32. prbf_pc_apply computes z = B r (host vectors, caller
  * order). */
 int prbf_pc_setup(prbf_ctx* ctx, int precision);
+/* PCApply of that PCASM (2d/rbf_interpolation.cxx:213-229) */
 int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
 
 /* ---- batches of independent problems (no reference counterpart: the reference solves
@@ -239,6 +257,7 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
 int prbf_gpumatmult_2d(const float* tX, const float* tY, float* tW, const float* sX, const float* sY,
                        const float* sG, const int* offset, int iblok, float sigma, int numCluster,
                        int numTrunc);
+/* the 3D seam, 3d/gpumatmult.cu:73-75 (3d/matmultgpu.cxx:7 packs its arrays) */
 int prbf_gpumatmult_3d(const float* tX, const float* tY, const float* tZ, float* tW, const float* sX,
                        const float* sY, const float* sZ, const float* sG, const int* offset, int iblok,
                        float sigma, int numCluster, int numTrunc);
