@@ -147,6 +147,22 @@ def fp64_peak_tflops(torch):
     return best
 
 
+def hbm_view(bytes_per_launch, ms_per_launch):
+    """The matvec against the HBM roof: algorithmic bytes per launch (2D: x, y, g read and w
+    written, 32 B per point) over the launch time, against the measured copy bandwidth of
+    MEASURED_PEAKS.json (else the 6800 GB/s fallback). The sum is FP64-pipe bound; this
+    shows how far from memory-bound it is."""
+    peak, src = 6800.0, "fallback 6800 GB/s (no MEASURED_PEAKS.json)"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peak, src = float(json.load(fh)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, TypeError, ValueError):
+        pass
+    gbs = bytes_per_launch / (ms_per_launch * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": src, "bytes_per_launch": bytes_per_launch}
+
+
 def profile_traffic(name):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", name)
@@ -325,7 +341,8 @@ def run_ours(args, rank, world):
                      "symmetric": symmetric,
                      "note": ("achieved counts the reference's 15 flops per ordered pair; the symmetric sum "
                               "evaluates one exponential for both ordered pairs of a point pair") if symmetric else None,
-                     "traffic": profile_traffic("gauss_fp64_2d_N4e6.txt")},
+                     "traffic": profile_traffic("gauss_fp64_2d_N4e6.txt"),
+                     "hbm_view": hbm_view(32 * n, ms / args.steps)},
         "fp32_matvec_gpairs": fp32_gpairs,
         "wall_s_timed_region": t_wall,
     }

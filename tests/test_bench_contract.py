@@ -33,3 +33,12 @@ def test_clock_summary_reports_throttle_reasons():
     assert s["sm_mhz"] == 2010.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
     assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
     assert bench.Clocks(0).summary()["reasons"] == ["unsampled"]
+
+
+def test_hbm_view_of_the_matvec():
+    sys.path.insert(0, ROOT)
+    import bench
+    v = bench.hbm_view(32 * 4_000_000, 44.8)
+    assert v["bound"] == "hbm" and v["unit"] == "GB/s" and v["bytes_per_launch"] == 128_000_000
+    assert abs(v["achieved"] - 128e6 / 44.8e-3 / 1e9) < 1e-9
+    assert v["peak"] > 0 and abs(v["frac"] - v["achieved"] / v["peak"]) < 1e-12
