@@ -250,7 +250,11 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
  * sources; iblok <= numCluster, offset[iblok] <= numCluster*numTrunc). Writes
  * tW[128 b + i] = sum_j sG_j exp(-|t - s_j|^2 / (2 sigma^2)) / (2 pi sigma^2) for the
  * 128 * iblok slots (the 3D form keeps this 2D normalisation, as the reference's does).
- * FP32 arithmetic on the caller's coordinates. Host pointers; the call is synchronous and
+ * FP32 arithmetic on the caller's coordinates, the exponential on the special-function unit
+ * (ex2.approx, subnormal terms flushed to zero) where the reference calls exp: each slot is
+ * within 1e-5 x sum_j |sG_j phi_ij| of the exactly rounded sum of the same FP32 inputs and
+ * within 2e-5 (same measure) of the reference kernel's own output, not bit-identical to it.
+ * Host pointers; the call is synchronous and
  * returns a PRBF_* status (the reference's returns void and checks nothing). Device
  * buffers are grow-only and kept per device for the life of the process, as the
  * reference's statics are; concurrent calls are serialised. */
@@ -269,16 +273,18 @@ int prbf_gpumatmult_3d(const float* tX, const float* tY, const float* tZ, float*
  * the same order, as prbf_matvec_setup: perm_dev[k] = caller index of the k-th sorted
  * point, cell_start_dev[c] = first sorted position of cell c (ncell + 1 entries; the grid
  * is derived from the points' bounding box, so the caller passes the capacity it
- * allocated and receives ncell). All pointers are device pointers; stream may be null.
+ * allocated and receives ncell, also when that capacity is too small, so it learns what to
+ * allocate). All pointers are device pointers; stream may be null.
  * Every temporary comes from one fixed device array inside the library
  * (PRBF_STATIC_SORT_SCRATCH_MIB MiB, held on every GPU that loads the library until the
  * process exits). Limits: n <= PRBF_STATIC_SORT_MAX_POINTS and ncell + 1 <= 8,388,608;
- * beyond them the call returns PRBF_ERR_CAPACITY without touching the buffers. The first
+ * beyond them the call returns PRBF_ERR_CAPACITY without touching perm_dev or
+ * cell_start_dev (ncell_out is still written when the cell count is the limit hit). The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress) with that
  * device current; make that first call before any stream capture. All calls share the
  * array: calls that overlap on the GPU (other threads, other streams) race and must be
- * serialised by the caller. The call synchronises the stream once to read the bounding
- * box back. */
+ * serialised by the caller. The call synchronises the stream twice: to read the bounding
+ * box back, and to read the kernels' status word at the end. */
 #define PRBF_STATIC_SORT_MAX_POINTS 1048576
 #define PRBF_STATIC_SORT_SCRATCH_MIB 13
 int prbf_cell_sort_static(int dim, int n, const double* x_dev, const double* y_dev, const double* z_dev,

@@ -18,6 +18,15 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# Where the reference's sources are read from: $PETRBF_REFERENCE_TREE, else the read-only
+# checkout this recipe was written against. Absent on machines that only run the tests.
+REFERENCE_TREE_DEFAULT = "/root/reference"
+
+
+def reference_tree():
+    """The reference checkout to compile from, or None where there is none."""
+    root = os.environ.get("PETRBF_REFERENCE_TREE", REFERENCE_TREE_DEFAULT)
+    return root if os.path.isdir(root) else None
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp"]
 
 

@@ -314,6 +314,7 @@ void scatter_dev(int n, const int* perm, const double* in, double* out, cudaStre
 // it never calls cudaMalloc or cudaFree. The array lives on every GPU that loads the
 // library until the process exits; all calls share it.
 #include <mutex>
+#include <new>
 
 #include "context.h"
 
@@ -348,7 +349,10 @@ int static_scratch(unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_static_mu);
   if (!g_static_addr[dev]) {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_static_sort_scratch) != cudaSuccess || !p) return PRBF_ERR_CUDA;
+    if (cudaGetSymbolAddress(&p, g_static_sort_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();  // leave no stale error for a later launch check
+      return PRBF_ERR_CUDA;
+    }
     g_static_addr[dev] = (unsigned char*)p;
   }
   *out = g_static_addr[dev];
@@ -410,6 +414,9 @@ extern "C" int prbf_cell_sort_static(int dim, int n, const double* x, const doub
     PRBF_CUDA(cudaMemcpyAsync(b, bbox, sizeof(b), cudaMemcpyDeviceToHost, s));
     PRBF_CUDA(cudaStreamSynchronize(s));
     Grid g = make_grid(dim, b, sigma, nsigma_box, sigma_buffer, sigma_trunc);
+    // the grid follows from the points' bounding box: report its size before any capacity
+    // refusal, so that a caller whose cell_start buffer is too short learns what to allocate
+    if (ncell_out) *ncell_out = g.ncell;
     if ((long long)g.ncell + 1 > cell_start_len || (long long)g.ncell + 1 > kStaticMaxScan)
       return PRBF_ERR_CAPACITY;
     PRBF_CUDA(cudaMemsetAsync(cell_start, 0, sizeof(int) * ((size_t)g.ncell + 1), s));
@@ -436,10 +443,14 @@ extern "C" int prbf_cell_sort_static(int dim, int n, const double* x, const doub
     PRBF_CUDA(cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     PRBF_CUDA(cudaStreamSynchronize(s));
     if (herr & DEV_ERR_RANGE) return PRBF_ERR_RANGE;
-    if (ncell_out) *ncell_out = g.ncell;
+    if (herr & DEV_ERR_TIMEOUT) return PRBF_ERR_TIMEOUT;
+    if (herr & (DEV_ERR_CAPACITY | DEV_ERR_INDEX)) return PRBF_ERR_CAPACITY;
+    if (herr) return PRBF_ERR_CUDA;  // no other bit is raised by these kernels
     return PRBF_OK;
   } catch (const Error& e) {
     return e.status;
+  } catch (const std::bad_alloc&) {
+    return PRBF_ERR_CAPACITY;  // host memory exhausted
   } catch (const std::exception&) {
     return PRBF_ERR_ARG;
   }

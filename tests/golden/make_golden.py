@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import oracle as O  # noqa: E402
+from oracle import build as _build  # noqa: E402
 from petrbf_gb300 import workloads as W  # noqa: E402
 
 
@@ -111,4 +112,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else _build.reference_tree()
+    if not root:
+        sys.exit("no reference tree: pass its path or set PETRBF_REFERENCE_TREE")
+    main(root)

@@ -19,14 +19,19 @@ MAX_POINTS = 1048576  # PRBF_STATIC_SORT_MAX_POINTS
 
 def _cases():
     x3, y3, z3, h3 = W.lattice_3d(40, jitter=0.25, seed=9)
+    # a sparse 3D cloud in cells of 0.01: 200^3 = 8,000,000 cells, so the cell-start scan
+    # needs its second level (more than 2048 x 2048 entries)
+    rs = np.random.default_rng(17)
+    xs, ys, zs = (rs.uniform(-1.0, 1.0, 5000) for _ in range(3))
     return [
         (2, W.lamb_oseen_lattice_1e4().x, W.lamb_oseen_lattice_1e4().y, None, (0.025, 8, 24, 24)),
         (2, *W.lattice_2d(1000, jitter=0.25, seed=3)[:2], None, (1.25e-3 * 2, 8, 24, 24)),
         (3, x3, y3, z3, (h3 / 0.8, 2, 10, 16)),
+        (3, xs, ys, zs, (0.01, 1, 3, 3)),
     ]
 
 
-@pytest.mark.parametrize("case", range(3))
+@pytest.mark.parametrize("case", range(4))
 def test_static_sort_equals_allocating_sort_on_two_calls(case):
     torch = pytest.importorskip("torch")
     dim, x, y, z, prm = _cases()[case]
@@ -72,6 +77,9 @@ def test_static_sort_rejects_sizes_beyond_its_limits():
     yd = torch.tensor(p.y, device="cuda")
     perm = torch.empty(p.n, dtype=torch.int32, device="cuda")
     cs = torch.empty(8, dtype=torch.int32, device="cuda")
+    ncell.value = -1
     st = L.prbf_cell_sort_static(2, p.n, xd.data_ptr(), yd.data_ptr(), None, p.sigma, 8, 24, 24,
                                  perm.data_ptr(), cs.data_ptr(), cs.numel(), ctypes.byref(ncell), None)
     assert st == N.ERR_CAPACITY
+    # the refusal still reports the grid's size, so the caller can allocate and call again
+    assert ncell.value == 100
