@@ -182,6 +182,21 @@ int prbf_get_trunc_counts(prbf_ctx* ctx, int* counts_out);
 int prbf_pc_setup(prbf_ctx* ctx, int precision);
 /* PCApply of that PCASM (2d/rbf_interpolation.cxx:213-229) */
 int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z);
+/* Read-back of the Schwarz subdomains built by prbf_pc_setup (no counterpart in the
+ * reference, whose blocks live inside PETSc): the buffer lists of Get_buffer::get_buffer
+ * (2d/get_buffer.h:9-90) -- off_out[c] .. off_out[c+1]-1 (ncell + 1 entries; ncell from
+ * prbf_matvec_info) index idx_out, which holds each cell's subdomain as sorted positions,
+ * centre points first, in the reference's order. Either pointer may be null (call once with
+ * idx_out null to learn off_out[ncell]). */
+int prbf_pc_buffer_lists(prbf_ctx* ctx, long long* off_out, int* idx_out);
+/* One subdomain block of cell `cell` (mysubmat, 2d/matmult.cxx:83-93): nb_out / nc_out its
+ * size and centre-point count; K_out (nb x nb, nullable) the block as the FP64 factorisation
+ * assembles it, K = 2 pi sigma^2 A_c, rows and columns in the factorisation's order
+ * (neighbour points -- buffer entries nc .. nb-1 -- first, then the centre points), before
+ * any diagonal shift; L_out (nb (nb + 1) / 2, nullable, FP64 set-up only) the packed factor
+ * as the apply reads it: row i holds L[i][0..i-1] and then 1 / L[i][i], where L L^T = A_c in
+ * that order. Returns PRBF_ERR_STATE for L_out after a mixed-precision set-up. */
+int prbf_pc_block(prbf_ctx* ctx, int cell, int* nb_out, int* nc_out, double* K_out, double* L_out);
 
 /* ---- batches of independent problems (no reference counterpart: the reference solves
  * one problem per call; this is the replica form for many small problems on one GPU) ---- */
@@ -294,5 +309,9 @@ int prbf_cell_sort_static(int dim, int n, const double* x_dev, const double* y_d
 
 #ifdef __cplusplus
 }
+/* The same entry under the reference's own name and C++ linkage (3d/wrapper.cxx:20-23):
+ * a caller that linked librbf.a keeps its declaration and call and links this library. */
+int RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, float* zg, float* wg, int np, float* xp,
+                     float* yp, float* zp, float* gp, float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc);
 #endif
 #endif

@@ -51,6 +51,13 @@ def lib():
         _lib.orc_rasm_apply.argtypes = [ctypes.c_void_p, _D, _D]
         _lib.orc_rasm_destroy.argtypes = [ctypes.c_void_p]
         _lib.orc_rasm_set_type.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_rasm_create_kind.restype = ctypes.c_void_p
+        _lib.orc_rasm_block_info.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, _I, _I]
+        _lib.orc_rasm_factor_rows.argtypes = [ctypes.c_void_p, ctypes.c_int, _D]
+        _lib.orc_gmres_ex.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, _D, _D, _D, _I,
+                                      ctypes.c_void_p, _D, _D, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I, _I, _D,
+                                      ctypes.c_int]
         _lib.orc_gmres.argtypes = [ctypes.POINTER(Grid), ctypes.c_int, _D, _D, _D, _I,
                                    ctypes.c_void_p, _D, _D, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I, _I, _D]
@@ -181,18 +188,49 @@ def block(g, idx, xs, ys, zs):
     return A
 
 
-class Rasm:
-    """Restricted (or, with basic=True, basic) additive Schwarz with dense LU blocks."""
+def gpu_block(g, idx, nc, xs, ys, zs):
+    """The block K = 2 pi sigma^2 A_c of one buffer list (centre first, nc centre points) as
+    the GPU library assembles it: rows and columns neighbours first, its table exp; the full
+    symmetric nb x nb matrix."""
+    idx = np.ascontiguousarray(idx, np.int32)
+    nb = idx.shape[0]
+    K = np.zeros((nb, nb), np.float64)
+    _check(lib().orc_gpu_block(ctypes.byref(g), nb, int(nc), _i(idx), _d(_f64(xs)), _d(_f64(ys)),
+                               _d(_f64(zs)), _d(K)), "gpu_block")
+    return np.tril(K) + np.tril(K, -1).T
 
-    def __init__(self, g, xs, ys, zs, cs, basic=False):
+
+FACTORS = {"lu": 0, "chol": 1}
+
+
+class Rasm:
+    """Restricted (or, with basic=True, basic) additive Schwarz. factor "lu": dense LU with
+    partial pivoting (PETSc's, the reference's); "chol": the GPU library's block arithmetic
+    restated (table exp, neighbours first, ordered Cholesky, its substitution order)."""
+
+    def __init__(self, g, xs, ys, zs, cs, basic=False, factor="lu"):
         self.g = g
         self.keep = (_f64(xs), _f64(ys), _f64(zs), cs)
         st = ctypes.c_int(0)
-        self.h = lib().orc_rasm_create(ctypes.byref(g), len(xs), _d(self.keep[0]),
-                                       _d(self.keep[1]), _d(self.keep[2]), _i(cs),
-                                       ctypes.byref(st))
+        self.h = lib().orc_rasm_create_kind(ctypes.byref(g), len(xs), _d(self.keep[0]),
+                                            _d(self.keep[1]), _d(self.keep[2]), _i(cs),
+                                            FACTORS[factor], ctypes.byref(st))
         self.status = st.value
+        self.factor = factor
         lib().orc_rasm_set_type(self.h, 1 if basic else 0)
+
+    def block_info(self, cell):
+        nb, nc, ns = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().orc_rasm_block_info(self.h, int(cell), ctypes.byref(nb), ctypes.byref(nc),
+                                         ctypes.byref(ns)), "block_info")
+        return nb.value, nc.value, ns.value
+
+    def factor_rows(self, cell):
+        """factor "chol": the packed rows of a cell (row i: L_A[i][0..i-1], 1/L_A[i][i])."""
+        nb, _, _ = self.block_info(cell)
+        out = np.empty(nb * (nb + 1) // 2, np.float64)
+        _check(lib().orc_rasm_factor_rows(self.h, int(cell), _d(out)), "factor_rows")
+        return out
 
     def apply(self, r):
         r = _f64(r)
@@ -209,24 +247,29 @@ class Rasm:
 
 
 def gmres(g, xs, ys, zs, cs, rasm, b, x0=None, rtol=1e-13, abstol=1e-50, dtol=1e5,
-          restart=30, max_it=1000):
-    """GMRES(restart) with the RASM preconditioner on the left, in cell order."""
+          restart=30, max_it=1000, texp=False):
+    """GMRES(restart) with the RASM preconditioner on the left, in cell order; texp: the
+    Gaussian sums take the GPU library's table exp."""
     b = _f64(b)
     n = b.shape[0]
     x = np.zeros(n, np.float64)
     its = ctypes.c_int(0)
     reason = ctypes.c_int(0)
     hist = np.zeros(max_it + 2, np.float64)
-    lib().orc_gmres(ctypes.byref(g), n, _d(_f64(xs)), _d(_f64(ys)), _d(_f64(zs)), _i(cs),
-                    rasm.h, _d(b), _d(_f64(x0)), rtol, abstol, dtol, restart, max_it, _d(x),
-                    ctypes.byref(its), ctypes.byref(reason), _d(hist))
+    lib().orc_gmres_ex(ctypes.byref(g), n, _d(_f64(xs)), _d(_f64(ys)), _d(_f64(zs)), _i(cs),
+                       rasm.h, _d(b), _d(_f64(x0)), rtol, abstol, dtol, restart, max_it, _d(x),
+                       ctypes.byref(its), ctypes.byref(reason), _d(hist), 4 if texp else 0)
     return x, its.value, reason.value, hist[:its.value + 1].copy()
 
 
 def rbf_interpolation(x, y, z, f, sigma, nsigma_box, sigma_buffer, sigma_trunc, rtol=1e-13,
-                      restart=30, max_it=1000, pc="rasm"):
+                      restart=30, max_it=1000, pc="rasm", factor="lu", texp=False,
+                      reverse_sums=False):
     """Weights g with A g = f, in the caller's order (2d/rbf_interpolation.cxx:25-310);
-    pc "asm" selects basic additive Schwarz (-pc_asm_type basic)."""
+    pc "asm" selects basic additive Schwarz (-pc_asm_type basic); factor "chol" the GPU
+    library's block arithmetic instead of the reference's LU; texp its table exp in the
+    Gaussian sums; reverse_sums adds every row's terms last to first (same operator,
+    another rounding order)."""
     x, y, z, f = _f64(x), _f64(y), _f64(z), _f64(f)
     n = x.shape[0]
     gout = np.zeros(n, np.float64)
@@ -235,7 +278,9 @@ def rbf_interpolation(x, y, z, f, sigma, nsigma_box, sigma_buffer, sigma_trunc, 
     _check(lib().orc_rbf_interpolation(3 if z is not None else 2, n, _d(x), _d(y), _d(z),
                                        _d(f), sigma, nsigma_box, sigma_buffer, sigma_trunc,
                                        rtol, restart, max_it, _d(gout), ctypes.byref(its),
-                                       ctypes.byref(reason), 1 if pc == "asm" else 0),
+                                       ctypes.byref(reason),
+                                       (1 if pc == "asm" else 0) | (2 * FACTORS[factor]) | (4 if texp else 0)
+                                       | (8 if reverse_sums else 0)),
            "rbf_interpolation")
     return gout, its.value, reason.value
 

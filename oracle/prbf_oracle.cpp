@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -177,6 +178,230 @@ inline double phi(double sigma, double dx, double dy, double dz, int dim) {
   return exp(-(r2) / (2 * sigma * sigma)) / (2 * M_PI * sigma * sigma);
 }
 
+// ---------------------------------------------------------------------------------------
+// The GPU library's FP64 arithmetic for the Schwarz blocks, restated (the "chol" form).
+// The reference factors each block with PETSc's dense LU; the GPU library instead takes the
+// Cholesky factor of K = 2 pi sigma^2 A_c with the block's neighbour points first and its
+// centre points last, evaluates exp with its own table, and applies the factor by
+// substitutions in a fixed operation order. Restating that arithmetic here lets a test
+// compare the GPU's factors bit for bit and run GMRES with the same preconditioner, so the
+// two Krylov histories differ only by the rounding of the Gaussian sums and the dots.
+// ---------------------------------------------------------------------------------------
+
+// exp table of n = 1024 entries: tab[4 j + i] = 2^(-j/n) c_i, c_i the monomial coefficients
+// of the cubic through (r_k, e^(L r_k)) at the Chebyshev nodes r_k = cos((2k+1) pi/8) / 2
+// of [-1/2, 1/2], L = ln2/n (Newton divided differences, expanded), in long double.
+const double* exp_table() {
+  static double tab[4096];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const int NP = 4, NT = 1024;
+    const long double PI = 3.141592653589793238462643383279502884L;
+    const long double L = logl(2.0L) / NT;
+    long double xr[NP], dd[NP], c[NP];
+    for (int k = 0; k < NP; k++) {
+      xr[k] = 0.5L * cosl((2 * k + 1) * PI / (2 * NP));
+      dd[k] = expl(L * xr[k]);
+      c[k] = 0.0L;
+    }
+    for (int lev = 1; lev < NP; lev++)
+      for (int k = NP - 1; k >= lev; k--) dd[k] = (dd[k] - dd[k - 1]) / (xr[k] - xr[k - lev]);
+    for (int k = NP - 1; k >= 0; k--) {
+      for (int i = NP - 1; i > 0; i--) c[i] = c[i - 1] - xr[k] * c[i];
+      c[0] = dd[k] - xr[k] * c[0];
+    }
+    for (int j = 0; j < NT; j++) {
+      long double t = exp2l(-(long double)j / NT);
+      for (int i = 0; i < NP; i++) tab[j * NP + i] = (double)(t * c[i]);
+    }
+  });
+  return tab;
+}
+
+inline double kexp_of_sigma(double sigma) { return 1024.0 / (2.0 * sigma * sigma * 0.6931471805599453); }
+
+inline double pow2_lower(double v, int m) {  // v * 2^-m by the exponent field
+  uint64_t b;
+  memcpy(&b, &v, 8);
+  b -= (uint64_t)m << 52;
+  memcpy(&v, &b, 8);
+  return v;
+}
+
+// exp(-d2 / (2 sigma^2)), kexp = kexp_of_sigma(sigma): k = rint(kexp d2) by the 1.5 * 2^52
+// addition, r = k - kexp d2 in one rounding, k = 1024 m + j, 2^-m T[j] p(r) by Horner
+// (m capped at 900).
+inline double exp_neg_tab(double d2, double kexp) {
+  const double* tab = exp_table();
+  const double magic = 6755399441055744.0;
+  const double kd = std::fma(d2, kexp, magic);
+  uint64_t b;
+  memcpy(&b, &kd, 8);
+  const int kk = (int)(uint32_t)(b & 0xffffffffu);
+  const double r = std::fma(-d2, kexp, kd - magic);
+  const int m = std::min(kk >> 10, 900);
+  const double* c = tab + 4 * (kk & 1023);
+  double q = pow2_lower(c[3], m);
+  q = std::fma(r, q, pow2_lower(c[2], m));
+  q = std::fma(r, q, pow2_lower(c[1], m));
+  q = std::fma(r, q, pow2_lower(c[0], m));
+  return q;
+}
+
+// Buffer-list entry of block row i: neighbours (entries nc ..) first, then the centre.
+inline int gpu_row(int i, int nb, int nc) { return i < nb - nc ? nc + i : i - (nb - nc); }
+
+// K[i][j], j <= i, of the block whose buffer list (centre first) is id: the differences
+// as the reference forms them, |d|^2 = fma(dy, dy, dx dx) (+ fma(dz, dz, .)), the table
+// exp, plus shift on the diagonal. Row-major nb x nb, lower triangle written.
+void gpu_block_K(int dim, int nb, int nc, const int* id, const double* x, const double* y,
+                 const double* z, double kexp, double shift, double* K) {
+  for (int i = 0; i < nb; i++) {
+    const int a = id[gpu_row(i, nb, nc)];
+    for (int j = 0; j <= i; j++) {
+      const int b = id[gpu_row(j, nb, nc)];
+      const double dx = x[a] - x[b], dy = y[a] - y[b];
+      double r2 = std::fma(dy, dy, dx * dx);
+      if (dim == 3) {
+        const double dz = z[a] - z[b];
+        r2 = std::fma(dz, dz, r2);
+      }
+      double v = exp_neg_tab(r2, kexp);
+      if (i == j) v = v + shift;
+      K[(size_t)i * nb + j] = v;
+    }
+  }
+}
+
+// Unblocked right-looking Cholesky of K (lower, row-major) in the GPU's operation order:
+// pivot column j: s = sqrt(a_jj) (a non-positive pivot is taken as 1 and reported),
+// r = 1/s, l_ij = a_ij * r, then a_il = fma(-l_ij, l_lj, a_il) for j < l <= i. Every
+// entry thus receives fma updates for the columns before its own in ascending order and
+// is then scaled. This loop is the definition; chol_blocked below computes the same
+// operations per entry faster. The work array U is the transpose (U[j][i] = L[i][j]).
+bool chol_unblocked(int n, const double* K, double* U, double* L) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++) U[(size_t)j * n + i] = K[(size_t)i * n + j];
+  bool ok = true;
+  for (int j = 0; j < n; j++) {
+    double* uj = U + (size_t)j * n;
+    double d = uj[j];
+    if (!(d > 0.0)) {
+      ok = false;
+      d = 1.0;
+    }
+    const double sq = sqrt(d), rc = 1.0 / sq;
+    uj[j] = sq;
+    for (int i = j + 1; i < n; i++) uj[i] = uj[i] * rc;
+    for (int l = j + 1; l < n; l++) {
+      double* ul = U + (size_t)l * n;
+      const double f = uj[l];
+      for (int i = l; i < n; i++) ul[i] = std::fma(-f, uj[i], ul[i]);
+    }
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++) L[(size_t)i * n + j] = U[(size_t)j * n + i];
+  return ok;
+}
+
+// The same Cholesky, right-looking over panels of 16 columns, on the transposed work array
+// U (U[j][i] = L[i][j], row-major): the panel's columns are factored in order, each
+// updating the panel's later rows at once; then every row below the panel takes the
+// panel's 16 updates in ascending order while it sits in cache (each update one
+// vectorised pass over the row). Per entry this is chol_unblocked's operation sequence,
+// so the factors are bit-identical; the trailing rows are read once per panel instead of
+// once per column. Reads K's lower triangle; writes U.
+bool chol_blocked(int n, const double* K, double* U) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++) U[(size_t)j * n + i] = K[(size_t)i * n + j];
+  bool ok = true;
+  const int P = 16;
+  for (int j0 = 0; j0 < n; j0 += P) {
+    const int j1 = std::min(n, j0 + P);
+    for (int j = j0; j < j1; j++) {
+      double* uj = U + (size_t)j * n;
+      double d = uj[j];
+      if (!(d > 0.0)) {
+        ok = false;
+        d = 1.0;
+      }
+      const double sq = sqrt(d), rc = 1.0 / sq;
+      uj[j] = sq;
+      for (int i = j + 1; i < n; i++) uj[i] = uj[i] * rc;
+      for (int l = j + 1; l < j1; l++) {
+        double* ul = U + (size_t)l * n;
+        const double f = uj[l];
+        for (int i = l; i < n; i++) ul[i] = std::fma(-f, uj[i], ul[i]);
+      }
+    }
+    for (int l = j1; l < n; l++) {
+      double* ul = U + (size_t)l * n;
+      for (int j = j0; j < j1; j++) {
+        const double* uj = U + (size_t)j * n;
+        const double f = uj[l];
+        for (int i = l; i < n; i++) ul[i] = std::fma(-f, uj[i], ul[i]);
+      }
+    }
+  }
+  return ok;
+}
+
+// Factor of the block K (lower, row-major) packed as the apply reads it: row i =
+// L_A[i][0..i-1] followed by 1 / L_A[i][i], L_A = L_K * sc the factor of A = K / (2 pi
+// sigma^2). U: n x n scratch. Returns false on a non-positive pivot.
+bool gpu_chol_pack(int n, const double* K, double sc, double* U, double* Lp) {
+  const bool ok = chol_blocked(n, K, U);
+  for (int i = 0; i < n; i++) {
+    double* row = Lp + (size_t)i * (i + 1) / 2;
+    for (int j = 0; j < i; j++) row[j] = U[(size_t)j * n + i] * sc;
+    row[i] = 1.0 / (U[(size_t)i * n + i] * sc);
+  }
+  return ok;
+}
+
+// The GPU apply's substitutions on one block vector y (block order), packed factor Lp:
+// forward over the whole block in 32-row panels (inside a panel, y_i receives
+// fma(-l_ij, y_j, .) for ascending j and is then multiplied by the reciprocal pivot; a row
+// below the panel subtracts ((a0 + a1) + (a2 + a3)), a_s the fma chain over 8 entries of
+// the panel from zero), then the back substitution over rows b0 .. nb-1 in 32-row panels
+// from the bottom (inside a panel descending; a row above a panel subtracts the fma chain
+// over the panel's entries from zero).
+void gpu_tri_apply(int nb, int b0, const double* Lp, double* y) {
+  auto L = [&](long long i, long long j) { return Lp[i * (i + 1) / 2 + j]; };
+  for (int p0 = 0; p0 < nb; p0 += 32) {
+    const int np = std::min(32, nb - p0);
+    for (int i = p0; i < p0 + np; i++) {
+      double v = y[i];
+      for (int j = p0; j < i; j++) v = std::fma(-L(i, j), y[j], v);
+      y[i] = v * L(i, i);
+    }
+    for (int i = p0 + np; i < nb; i++) {
+      double a[4];
+      for (int sb = 0; sb < 4; sb++) {
+        double t = 0.0;
+        for (int q = 0; q < 8; q++) t = std::fma(L(i, p0 + 8 * sb + q), y[p0 + 8 * sb + q], t);
+        a[sb] = t;
+      }
+      y[i] = y[i] - ((a[0] + a[1]) + (a[2] + a[3]));
+    }
+  }
+  const int nback = nb - b0;
+  for (int pe = nback; pe > 0; pe -= 32) {
+    const int p0 = std::max(0, pe - 32), np = pe - p0;
+    const int o = b0 + p0;
+    for (int i = np - 1; i >= 0; i--) {
+      double v = y[o + i];
+      for (int j = np - 1; j > i; j--) v = std::fma(-L(o + j, o + i), y[o + j], v);
+      y[o + i] = v * L(o + i, o + i);
+    }
+    for (int k = 0; k < p0; k++) {
+      double acc = 0.0;
+      for (int j = 0; j < np; j++) acc = std::fma(L(o + j, b0 + k), y[o + j], acc);
+      y[b0 + k] = y[b0 + k] - acc;
+    }
+  }
+}
+
 // Deterministic sum: fixed 256 chunks summed in order, independent of thread count.
 double det_dot(int n, const double* a, const double* b) {
   const int nch = 256;
@@ -203,6 +428,10 @@ struct Rasm {
   std::vector<double> lu;             // LU factors (row-major)
   std::vector<int> piv;               // pivot rows, per block (offset = off)
   int basic = 0;                      // PETSc -pc_asm_type basic instead of restrict
+  int kind = 0;                       // 0: dense LU (the reference's); 1: the GPU's Cholesky
+  std::vector<long long> coff;        // kind 1: packed-factor offsets (nb (nb + 1) / 2 each)
+  std::vector<double> chol;           // kind 1: packed factors (gpu_chol_pack)
+  int nshifted = 0;                   // kind 1: blocks refactored with a diagonal shift
 };
 
 // Dense LU with partial pivoting (row interchanges), the algorithm PETSc's
@@ -257,7 +486,9 @@ void lu_solve(int n, const double* A, const int* piv, double* b) {
 
 void gauss_sum_impl(const orc_grid* g, const double* tx, const double* ty, const double* tz,
                     const int* cs_tgt, const double* sx, const double* sy, const double* sz,
-                    const double* sg, const int* cs_src, double* w) {
+                    const double* sg, const int* cs_src, double* w, bool texp = false,
+                    bool reverse = false) {
+  const double kexp = kexp_of_sigma(g->sigma);
 #pragma omp parallel
   {
     std::vector<int> list;
@@ -270,15 +501,16 @@ void gauss_sum_impl(const orc_grid* g, const double* tx, const double* ty, const
       // 2d/matmult.cxx:33-43 (3d/matmult.cxx:33-44)
       for (int i = cs_tgt[ic]; i < cs_tgt[ic + 1]; i++) {
         double acc = 0;
-        for (int t = 0; t < cnt; t++) {
-          int j = list[t];
+        for (int u = 0; u < cnt; u++) {
+          // reverse: the same terms summed last to first (a rounding-order probe)
+          int j = list[reverse ? cnt - 1 - u : u];
           double dx = tx[i] - sx[j];
           double dy = ty[i] - sy[j];
           // same grouping as the reference: (g * exp(.)) / (2 pi sigma^2)
           double r2 = g->dim == 3 ? dx * dx + dy * dy + (tz[i] - sz[j]) * (tz[i] - sz[j])
                                   : dx * dx + dy * dy;
-          acc += sg[j] * exp(-(r2) / (2 * g->sigma * g->sigma)) /
-                 (2 * M_PI * g->sigma * g->sigma);
+          const double e = texp ? exp_neg_tab(r2, kexp) : exp(-(r2) / (2 * g->sigma * g->sigma));
+          acc += sg[j] * e / (2 * M_PI * g->sigma * g->sigma);
         }
         w[i] = acc;
       }
@@ -407,7 +639,50 @@ int orc_block(const orc_grid* g, int nb, const int* idx, const double* x, const 
 
 void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y,
                       const double* z, const int* cs, int* status) {
+  return orc_rasm_create_kind(g, n, x, y, z, cs, 0, status);
+}
+
+// kind 1: the GPU library's blocks (table exp, neighbours first, K = 2 pi sigma^2 A_c),
+// ordered Cholesky with the GPU's shifted retries (diagonal + 1e-12, then + 1e-9, relative
+// to K's unit diagonal) for blocks with a non-positive pivot, packed factors.
+static int rasm_build_chol(const orc_grid* g, Rasm* R, const std::vector<int>& cnt, const double* x,
+                           const double* y, const double* z) {
+  R->coff.assign(g->ncell + 1, 0);
+  for (int c = 0; c < g->ncell; c++)
+    R->coff[c + 1] = R->coff[c] + (long long)cnt[c] * (cnt[c] + 1) / 2;
+  R->chol.resize(R->coff[g->ncell]);
+  const double kexp = kexp_of_sigma(g->sigma);
+  const double out_scale = 2.0 * M_PI * g->sigma * g->sigma;
+  const double sc = sqrt(1.0 / out_scale);
+  int bad = 0, shifted = 0;
+#pragma omp parallel reduction(| : bad) reduction(+ : shifted)
+  {
+    std::vector<double> K, U;
+#pragma omp for schedule(dynamic, 1)
+    for (int c = 0; c < g->ncell; c++) {
+      const int nb = cnt[c];
+      if (!nb) continue;
+      const int nc = R->cs[c + 1] - R->cs[c];
+      K.resize((size_t)nb * nb);
+      U.resize((size_t)nb * nb);
+      bool ok = false;
+      for (int attempt = 0; attempt < 3 && !ok; attempt++) {
+        const double shift = attempt == 0 ? 0.0 : (attempt == 1 ? 1e-12 : 1e-9);
+        gpu_block_K(g->dim, nb, nc, R->idx.data() + R->off[c], x, y, z, kexp, shift, K.data());
+        ok = gpu_chol_pack(nb, K.data(), sc, U.data(), R->chol.data() + R->coff[c]);
+        if (!ok && attempt == 0) shifted++;
+      }
+      if (!ok) bad = 1;
+    }
+  }
+  R->nshifted = shifted;
+  return bad ? ERR_SINGULAR : OK;
+}
+
+void* orc_rasm_create_kind(const orc_grid* g, int n, const double* x, const double* y,
+                           const double* z, const int* cs, int kind, int* status) {
   Rasm* R = new Rasm;
+  R->kind = kind == 1 ? 1 : 0;
   R->n = n;
   R->ncell = g->ncell;
   R->cs.assign(cs, cs + g->ncell + 1);
@@ -422,8 +697,13 @@ void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y
     R->aoff[c + 1] = R->aoff[c] + (long long)cnt[c] * cnt[c];
   }
   R->idx.resize(R->off[g->ncell]);
-  R->piv.resize(R->off[g->ncell]);
   orc_buffer_fill(g, x, y, z, cs, R->off.data(), R->idx.data());
+  if (R->kind == 1) {
+    int st = rasm_build_chol(g, R, cnt, x, y, z);
+    if (status) *status = st;
+    return R;
+  }
+  R->piv.resize(R->off[g->ncell]);
   R->lu.resize(R->aoff[g->ncell]);
   int bad = 0;
   // mysubmat (2d/matmult.cxx:53-104) + the per-block dense LU of -sub_pc_type lu.
@@ -456,6 +736,14 @@ static void asm_basic_apply(const Rasm* R, const double* r, double* out) {
     if (!nb) continue;
     double* buf = sol.data() + R->off[c];
     const int* id = R->idx.data() + R->off[c];
+    if (R->kind == 1) {
+      const int nc = R->cs[c + 1] - R->cs[c];
+      std::vector<double> yb(nb);
+      for (long long j = 0; j < nb; j++) yb[j] = r[id[gpu_row((int)j, (int)nb, nc)]];
+      gpu_tri_apply((int)nb, 0, R->chol.data() + R->coff[c], yb.data());
+      for (long long j = 0; j < nb; j++) buf[gpu_row((int)j, (int)nb, nc)] = yb[j];
+      continue;
+    }
     for (long long i = 0; i < nb; i++) buf[i] = r[id[i]];
     lu_solve((int)nb, R->lu.data() + R->aoff[c], R->piv.data() + R->off[c], buf);
   }
@@ -480,9 +768,16 @@ int orc_rasm_apply(void* h, const double* r, double* out) {
       if (!nb) continue;
       buf.resize(nb);
       const int* id = R->idx.data() + R->off[c];
+      int nc = R->cs[c + 1] - R->cs[c];
+      if (R->kind == 1) {
+        const int n1 = (int)nb - nc;
+        for (long long j = 0; j < nb; j++) buf[j] = r[id[gpu_row((int)j, (int)nb, nc)]];
+        gpu_tri_apply((int)nb, n1, R->chol.data() + R->coff[c], buf.data());
+        for (int i = 0; i < nc; i++) out[R->cs[c] + i] = buf[n1 + i];
+        continue;
+      }
       for (long long i = 0; i < nb; i++) buf[i] = r[id[i]];
       lu_solve((int)nb, R->lu.data() + R->aoff[c], R->piv.data() + R->off[c], buf.data());
-      int nc = R->cs[c + 1] - R->cs[c];
       for (int i = 0; i < nc; i++) out[R->cs[c] + i] = buf[i];
     }
   }
@@ -490,6 +785,43 @@ int orc_rasm_apply(void* h, const double* r, double* out) {
 }
 
 void orc_rasm_destroy(void* h) { delete (Rasm*)h; }
+
+int orc_rasm_block_info(void* h, int cell, int* nb, int* nc, int* nshifted) {
+  Rasm* R = (Rasm*)h;
+  if (!R || cell < 0 || cell >= R->ncell) return ERR_ARG;
+  if (nb) *nb = (int)(R->off[cell + 1] - R->off[cell]);
+  if (nc) *nc = R->cs[cell + 1] - R->cs[cell];
+  if (nshifted) *nshifted = R->nshifted;
+  return OK;
+}
+
+int orc_rasm_factor_rows(void* h, int cell, double* out) {
+  Rasm* R = (Rasm*)h;
+  if (!R || R->kind != 1 || cell < 0 || cell >= R->ncell) return ERR_ARG;
+  std::copy(R->chol.begin() + R->coff[cell], R->chol.begin() + R->coff[cell + 1], out);
+  return OK;
+}
+
+// The blocked Cholesky against its definition on one SPD block K (n x n, row-major lower
+// read; the full matrix is not modified): 1 if every entry of the two factors is
+// bit-identical (and both report the same pivot status), else 0.
+int orc_chol_blocked_matches_unblocked(int n, const double* K) {
+  std::vector<double> U1((size_t)n * n), L1((size_t)n * n), U2((size_t)n * n);
+  const bool ok1 = chol_unblocked(n, K, U1.data(), L1.data());
+  const bool ok2 = chol_blocked(n, K, U2.data());
+  if (ok1 != ok2) return 0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++)
+      if (memcmp(&L1[(size_t)i * n + j], &U2[(size_t)j * n + i], sizeof(double)) != 0) return 0;
+  return 1;
+}
+
+int orc_gpu_block(const orc_grid* g, int nb, int nc, const int* idx, const double* x, const double* y,
+                  const double* z, double* K) {
+  if (!g || nb <= 0 || nc < 0 || nc > nb) return ERR_ARG;
+  gpu_block_K(g->dim, nb, nc, idx, x, y, z, kexp_of_sigma(g->sigma), 0.0, K);
+  return OK;
+}
 
 // GMRES(restart), left preconditioning, classical Gram-Schmidt without refinement,
 // Givens rotations, preconditioned-residual convergence test relative to the first
@@ -500,13 +832,25 @@ int orc_gmres(const orc_grid* g, int n, const double* x, const double* y, const 
               const int* cs, void* rasm, const double* b, const double* x0, double rtol,
               double abstol, double dtol, int restart, int max_it, double* xsol, int* its_out,
               int* reason_out, double* hist) {
+  return orc_gmres_ex(g, n, x, y, z, cs, rasm, b, x0, rtol, abstol, dtol, restart, max_it, xsol,
+                      its_out, reason_out, hist, 0);
+}
+
+// flags bit 2: the Gaussian sums take the GPU library's table exp instead of libm's exp;
+// bit 3: every row of the sums adds its terms in reverse order (same terms, another
+// rounding order -- shows how far the stopping point moves with rounding alone).
+int orc_gmres_ex(const orc_grid* g, int n, const double* x, const double* y, const double* z,
+                 const int* cs, void* rasm, const double* b, const double* x0, double rtol,
+                 double abstol, double dtol, int restart, int max_it, double* xsol, int* its_out,
+                 int* reason_out, double* hist, int flags) {
+  const bool texp = (flags & 4) != 0, rev = (flags & 8) != 0;
   const double haptol = 1e-30;
   int m = restart;
   std::vector<double> V((size_t)(m + 1) * n), t(n), w(n);
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cc(m), ss(m), grs(m + 1);
   for (int i = 0; i < n; i++) xsol[i] = x0 ? x0[i] : 0.0;
   auto apply_BA = [&](const double* v, double* out) {
-    gauss_sum_impl(g, x, y, z, cs, x, y, z, v, cs, t.data());
+    gauss_sum_impl(g, x, y, z, cs, x, y, z, v, cs, t.data(), texp, rev);
     orc_rasm_apply(rasm, t.data(), out);
   };
   int its = 0, reason = 0;
@@ -523,7 +867,7 @@ int orc_gmres(const orc_grid* g, int n, const double* x, const double* y, const 
   };
   while (!reason) {
     // v0 = B (b - A x)
-    gauss_sum_impl(g, x, y, z, cs, x, y, z, xsol, cs, t.data());
+    gauss_sum_impl(g, x, y, z, cs, x, y, z, xsol, cs, t.data(), texp, rev);
     for (int i = 0; i < n; i++) w[i] = b[i] - t[i];
     double* v0 = V.data();
     orc_rasm_apply(rasm, w.data(), v0);
@@ -611,7 +955,8 @@ int orc_gmres(const orc_grid* g, int n, const double* x, const double* y, const 
 int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, const double* z,
                           const double* f, double sigma, int nsigma_box, int sigma_buffer,
                           int sigma_trunc, double rtol, int restart, int max_it, double* g_out,
-                          int* its, int* reason, int pc_basic) {
+                          int* its, int* reason, int pc_flags) {
+  const int pc_basic = pc_flags & 1;
   if (n <= 0) return ERR_ARG;
   double b[6] = {x[0], x[0], y[0], y[0], dim == 3 ? z[0] : 0, dim == 3 ? z[0] : 0};
   for (int i = 0; i < n; i++) {
@@ -639,14 +984,14 @@ int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, cons
     fs[k] = f[perm[k]];
   }
   const double* zp = dim == 3 ? zs.data() : nullptr;
-  void* R = orc_rasm_create(&g, n, xs.data(), ys.data(), zp, cs.data(), &st);
+  void* R = orc_rasm_create_kind(&g, n, xs.data(), ys.data(), zp, cs.data(), (pc_flags & 2) ? 1 : 0, &st);
   if (st) {
     orc_rasm_destroy(R);
     return st;
   }
   orc_rasm_set_type(R, pc_basic);
-  orc_gmres(&g, n, xs.data(), ys.data(), zp, cs.data(), R, fs.data(), nullptr, rtol, 1e-50,
-            1e5, restart, max_it, gs.data(), its, reason, nullptr);
+  orc_gmres_ex(&g, n, xs.data(), ys.data(), zp, cs.data(), R, fs.data(), nullptr, rtol, 1e-50,
+               1e5, restart, max_it, gs.data(), its, reason, nullptr, pc_flags);
   orc_rasm_destroy(R);
   for (int k = 0; k < n; k++) g_out[perm[k]] = gs[k];
   return OK;

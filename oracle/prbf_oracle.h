@@ -2,7 +2,8 @@
  * prbf_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement of PetRBF's solve path (cell list, truncation and buffer sets,
- * truncated Gaussian matvec, dense subdomain blocks, dense LU with partial pivoting,
+ * truncated Gaussian matvec, dense subdomain blocks, dense LU with partial pivoting (and,
+ * as a second form, the GPU library's own block Cholesky arithmetic restated),
  * restricted additive Schwarz, GMRES(restart) with left preconditioning, evaluation).
  * It is the checker for the CUDA path and the timed CPU baseline; the product never
  * links, loads or calls it.
@@ -61,6 +62,20 @@ int orc_block(const orc_grid* g, int nb, const int* idx, const double* x,
 
 void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y,
                       const double* z, const int* cs, int* status);
+/* kind 0: dense LU with partial pivoting (PETSc's -sub_pc_type lu, the reference's);
+ * kind 1: the GPU library's arithmetic -- blocks K = 2 pi sigma^2 A_c with the neighbour
+ * points first, its table exp, the ordered Cholesky and the apply's substitution order. */
+void* orc_rasm_create_kind(const orc_grid* g, int n, const double* x, const double* y,
+                           const double* z, const int* cs, int kind, int* status);
+int orc_rasm_block_info(void* h, int cell, int* nb, int* nc, int* nshifted);
+/* kind 1: the packed factor rows of a cell (row i: L_A[i][0..i-1], 1/L_A[i][i]) */
+int orc_rasm_factor_rows(void* h, int cell, double* out);
+/* 1 if kind 1's blocked Cholesky reproduces the unblocked loop it restates bit for bit on
+ * the SPD matrix K (n x n row-major, lower triangle read) */
+int orc_chol_blocked_matches_unblocked(int n, const double* K);
+/* kind 1's block K (nb x nb row-major, lower triangle, neighbours first) of one buffer list */
+int orc_gpu_block(const orc_grid* g, int nb, int nc, const int* idx, const double* x,
+                  const double* y, const double* z, double* K);
 int orc_rasm_apply(void* h, const double* r, double* out);
 int orc_rasm_set_type(void* h, int basic);  /* 1: basic additive Schwarz (-pc_asm_type basic) */
 void orc_rasm_destroy(void* h);
@@ -70,11 +85,19 @@ int orc_gmres(const orc_grid* g, int n, const double* x, const double* y,
               const double* x0, double rtol, double abstol, double dtol, int restart,
               int max_it, double* xsol, int* its, int* reason, double* hist);
 
+int orc_gmres_ex(const orc_grid* g, int n, const double* x, const double* y,
+                 const double* z, const int* cs, void* rasm, const double* b,
+                 const double* x0, double rtol, double abstol, double dtol, int restart,
+                 int max_it, double* xsol, int* its, int* reason, double* hist, int flags);
+
+/* pc_flags: bit 0 basic additive Schwarz (-pc_asm_type basic); bit 1 the GPU's Cholesky
+ * blocks (kind 1) instead of LU; bit 2 the GPU's table exp in the Gaussian sums; bit 3 the
+ * sums' terms added in reverse order (a rounding-order probe). */
 int orc_rbf_interpolation(int dim, int n, const double* x, const double* y,
                           const double* z, const double* f, double sigma,
                           int nsigma_box, int sigma_buffer, int sigma_trunc,
                           double rtol, int restart, int max_it, double* g_out,
-                          int* its, int* reason, int pc_basic);
+                          int* its, int* reason, int pc_flags);
 int orc_vorticity_evaluation(int dim, int nt, const double* xt, const double* yt,
                              const double* zt, int ns, const double* xs,
                              const double* ys, const double* zs, const double* gs,

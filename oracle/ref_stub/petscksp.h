@@ -5,8 +5,10 @@
  * buffer, matvec, block and evaluation code makes (2d|3d/get_cluster.h,
  * get_trunc.h, get_buffer.h, get_vorticity.h, matmult.cxx), on one process with
  * plain dense storage, so those files compile unmodified and produce golden vectors.
- * KSP/PC are deliberately absent: the Krylov solver and PCASM are not exercised
- * through this stand-in.
+ * KSP and PCASM are deliberately absent: the Krylov solver is not exercised through this
+ * stand-in. The few extra Vec/Mat/PC shell calls at the end let the package's PETSc glue
+ * (petrbf_gb300/glue/petrbf_petsc.cxx) compile and run against it in the tests, with the
+ * signatures PETSc declares for them.
  */
 #ifndef PRBF_REF_STUB_PETSCKSP_H
 #define PRBF_REF_STUB_PETSCKSP_H
@@ -81,4 +83,15 @@ static inline PetscErrorCode MatSetValues(Mat m, PetscInt nr, const PetscInt* ir
 static inline PetscErrorCode MatAssemblyBegin(Mat, MatAssemblyType) { return 0; }
 static inline PetscErrorCode MatAssemblyEnd(Mat, MatAssemblyType) { return 0; }
 static inline PetscErrorCode MatDestroy(Mat* m) { delete *m; *m = nullptr; return 0; }
+
+// ---- for the PETSc glue of the package (one process: local = global sizes) ----------
+#define PETSC_ERR_LIB 76
+struct _p_PC { void* ctx = nullptr; };
+typedef _p_PC* PC;
+static inline PetscErrorCode VecGetLocalSize(Vec v, PetscInt* n) { *n = (PetscInt)v->a.size(); return 0; }
+static inline PetscErrorCode VecGetArrayRead(Vec v, const PetscScalar** p) { *p = v->a.data(); return 0; }
+static inline PetscErrorCode VecRestoreArrayRead(Vec, const PetscScalar**) { return 0; }
+static inline PetscErrorCode MatShellSetContext(Mat m, void* c) { m->ctx = c; return 0; }
+static inline PetscErrorCode PCShellGetContext(PC pc, void* c) { *(void**)c = pc->ctx; return 0; }
+static inline PetscErrorCode PCShellSetContext(PC pc, void* c) { pc->ctx = c; return 0; }
 #endif

@@ -90,6 +90,8 @@ SIGNATURES = {
     "prbf_get_trunc_counts": (ctypes.c_int, [ctypes.c_void_p, _I]),
     "prbf_pc_setup": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "prbf_pc_apply": (ctypes.c_int, [ctypes.c_void_p, _D, _D]),
+    "prbf_pc_buffer_lists": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I]),
+    "prbf_pc_block": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _I, _I, _D, _D]),
     "prbf_cell_sort_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

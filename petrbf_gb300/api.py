@@ -148,6 +148,30 @@ class Context:
         self._check(N.lib().prbf_pc_apply(self.h, _ptr(r), _ptr(out)))
         return out
 
+    def pc_buffer_lists(self):
+        """The Schwarz subdomains of the last pc_setup (Get_buffer::get_buffer): offsets
+        (ncell + 1) and the sorted positions of every cell's subdomain, centre first."""
+        ncell = self.matvec_info()["ncell"]
+        off = np.empty(ncell + 1, np.int64)
+        self._check(N.lib().prbf_pc_buffer_lists(self.h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                                  None))
+        idx = np.empty(max(int(off[-1]), 1), np.int32)
+        self._check(N.lib().prbf_pc_buffer_lists(self.h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                                  idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return off, idx[:int(off[-1])]
+
+    def pc_block(self, cell, block=True, factor=True):
+        """(nb, nc, K, L) of one subdomain: K = 2 pi sigma^2 A_c as the FP64 factorisation
+        assembles it (neighbour points first, then the centre), L the packed factor rows as
+        stored (row i: L[i][0..i-1], 1/L[i][i]; FP64 set-up only)."""
+        nb, nc = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(N.lib().prbf_pc_block(self.h, int(cell), ctypes.byref(nb), ctypes.byref(nc), None, None))
+        K = np.empty((nb.value, nb.value), np.float64) if block else None
+        L = np.empty(nb.value * (nb.value + 1) // 2, np.float64) if factor else None
+        if nb.value:
+            self._check(N.lib().prbf_pc_block(self.h, int(cell), None, None, _ptr(K), _ptr(L)))
+        return nb.value, nc.value, K, L
+
     # ---- solve and evaluation -------------------------------------------------------
     def interpolate(self, x, y, z, f):
         """Weights g with A g = f (f may hold several right-hand sides as columns)."""

@@ -131,6 +131,38 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, unsigne
   return false;
 }
 
+// 1024 / (2 sigma^2 ln2): the exponent factor of exp_neg_tab (the host computes the same
+// expression for single problems; products and a division only, so nothing is fused).
+__host__ __device__ __forceinline__ double kexp_of_sigma(double sigma) {
+  return 1024.0 / (2.0 * sigma * sigma * 0.6931471805599453);
+}
+
+// v * 2^-m for a normal v whose exponent stays normal (m20 = m << 20): the exponent field
+// is lowered by m, exactly.
+__device__ __forceinline__ double pow2_lower(double v, int m20) {
+  return __hiloint2double(__double2hiint(v) - m20, __double2loint(v));
+}
+
+// exp(-d2 / (2 sigma^2)) from the sums' FP64 table (exp_table_dev: n = 1024, tab[4j + i] =
+// 2^(-j/n) c_i, c_i the cubic through e^(L r) at the Chebyshev nodes of [-1/2, 1/2], L =
+// ln2/n), with kexp = n / (2 sigma^2 ln2): k = rint(kexp d2), r = k - kexp d2 (one rounding),
+// k = n m + j, result 2^-m (T[j] p(r)) by Horner with every operation written out, so a CPU
+// restatement with the same table reproduces it bit for bit. m is capped at 900 (2^-900 ~
+// 1e-271) so the scaled coefficients stay normal; the blocks never reach the cap.
+__device__ __forceinline__ double exp_neg_tab(double d2, double kexp, const double* __restrict__ tab) {
+  const double magic = 6755399441055744.0;  // 1.5 * 2^52: rint by addition
+  const double kd = __fma_rn(d2, kexp, magic);
+  const int kk = __double2loint(kd);
+  const double r = __fma_rn(-d2, kexp, __dsub_rn(kd, magic));
+  const int m20 = min(kk >> 10, 900) << 20;
+  const double* c = tab + 4 * (kk & 1023);
+  double q = pow2_lower(c[3], m20);
+  q = __fma_rn(r, q, pow2_lower(c[2], m20));
+  q = __fma_rn(r, q, pow2_lower(c[1], m20));
+  q = __fma_rn(r, q, pow2_lower(c[0], m20));
+  return q;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -142,4 +142,10 @@ void gauss_sum_dev(const GaussPlan& plan, const PointsView& tgt, const PointsVie
                    const double* g, double* w, bool fp32, unsigned* err, cudaStream_t s,
                    const int* skip = nullptr, int nv = 1, long long vstride = 0);
 
+// Device address of the FP64 exponential table of the sums (n = 1024 entries of the
+// T[j]-folded cubic, 4 coefficients each), uploaded to the current device on first use.
+// Kernels of other files use it through exp_neg_tab (common.cuh), so every FP64 Gaussian
+// of the library evaluates exp the same way.
+const double* exp_table_dev(cudaStream_t s);
+
 }  // namespace prbf

@@ -1693,4 +1693,20 @@ void gauss_sum_dev(const GaussPlan& P, const PointsView& t, const PointsView& s,
   }
 }
 
+const double* exp_table_dev(cudaStream_t s) {
+  static std::atomic<const double*> addr[64];
+  int dev = 0;
+  PRBF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw Error(PRBF_ERR_CUDA, "device index beyond the table cache");
+  upload_table(s);
+  const double* p = addr[dev].load();
+  if (!p) {
+    void* q = nullptr;
+    PRBF_CUDA(cudaGetSymbolAddress(&q, d_tab_big));
+    p = (const double*)q;
+    addr[dev].store(p);
+  }
+  return p;
+}
+
 }  // namespace prbf

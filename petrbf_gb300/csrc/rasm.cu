@@ -46,8 +46,11 @@ struct SP {  // padded shared row strides (16-byte aligned rows)
 };
 
 // ---- buffer lists ------------------------------------------------------------------
-// One warp per cell. mode 0: count; mode 1: fill idx[boff[c] ...] in order (centre
-// first, then the column ranges of the neighbour window).
+// One warp per cell. mode 0: count; mode 1: fill idx[boff[c] ...] in the reference's
+// order (2d/get_buffer.h:31-77, 3d twin): the centre points first, then the neighbour
+// cells in jx, jy (, jz) order, each cell's points ascending. In 2D the cells jy0 .. jy1
+// of a column jx are one contiguous range of the sorted points; in 3D (cell index
+// iz nx ny + ix ny + iy) consecutive jz are not, so the window is walked cell by cell.
 __global__ void k_buffer_lists(Grid g, const double* __restrict__ x, const double* __restrict__ y,
                                const double* __restrict__ z, const int* __restrict__ cs, int mode,
                                int* __restrict__ cnt, const long long* __restrict__ boff,
@@ -75,21 +78,31 @@ __global__ void k_buffer_lists(Grid g, const double* __restrict__ x, const doubl
   for (int j = c0 + lane; j < c1; j += 32)
     if (mode) idx[pos + (j - c0)] = j;
   n = c1 - c0;
-  for (int jz = jz0; jz <= jz1; jz++)
-    for (int jx = jx0; jx <= jx1; jx++) {
-      int a = cs[cell_of(g, jx, jy0, jz)], b = cs[cell_of(g, jx, jy1, jz) + 1];
-      for (int j0 = a; j0 < b; j0 += 32) {
-        int j = j0 + lane;
-        bool in = false;
-        if (j < b && !(j >= c0 && j < c1)) {
-          in = fabs(x[j] - xc) < L && fabs(y[j] - yc) < L;
-          if (g.dim == 3) in = in && fabs(z[j] - zc) < L;
-        }
-        unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (mode && in) idx[pos + n + __popc(bal & ((1u << lane) - 1u))] = j;
-        n += __popc(bal);
+  // points [a, b) of the window that pass the buffer box test, in order (the centre
+  // cell's own points are skipped: they lead the list)
+  auto scan = [&](int a, int b) {
+    for (int j0 = a; j0 < b; j0 += 32) {
+      int j = j0 + lane;
+      bool in = false;
+      if (j < b && !(j >= c0 && j < c1)) {
+        in = fabs(x[j] - xc) < L && fabs(y[j] - yc) < L;
+        if (g.dim == 3) in = in && fabs(z[j] - zc) < L;
       }
+      unsigned bal = __ballot_sync(0xffffffffu, in);
+      if (mode && in) idx[pos + n + __popc(bal & ((1u << lane) - 1u))] = j;
+      n += __popc(bal);
     }
+  };
+  if (g.dim == 2) {
+    for (int jx = jx0; jx <= jx1; jx++) scan(cs[cell_of(g, jx, jy0, 0)], cs[cell_of(g, jx, jy1, 0) + 1]);
+  } else {
+    for (int jx = jx0; jx <= jx1; jx++)
+      for (int jy = jy0; jy <= jy1; jy++)
+        for (int jz = jz0; jz <= jz1; jz++) {
+          const int cc = cell_of(g, jx, jy, jz);
+          if (cc != c) scan(cs[cc], cs[cc + 1]);
+        }
+  }
   if (mode == 0 && lane == 0) cnt[c] = n;
 }
 
@@ -109,18 +122,23 @@ __global__ void k_split_hl(long long n, const double* __restrict__ v, float2* __
 // K[i][j] = exp(-|x_a - x_b|^2 / (2 sigma^2)) (+ shift on the diagonal), block order
 // neighbours first then centre: block row i < n1 -> buffer entry nc + i, else i - n1.
 // Lower triangle only (the factorisation reads nothing else). hl (FP32 form): the n
-// points' coordinates split by k_split_hl, dim arrays of n one after the other.
+// points' coordinates split by k_split_hl, dim arrays of n one after the other. FP64 form:
+// the differences as the reference forms them (x_a - x_b), |d|^2 = fma(dy, dy, dx dx)
+// (+ fma(dz, dz, .)), and the exponential of the sums' table (exp_neg_tab, kexp = 1024 /
+// (2 sigma^2 ln2)), every operation rounded as written.
 template <class T>
 __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const long long* __restrict__ boff,
                            const int* __restrict__ cs, const int* __restrict__ idx,
                            const long long* __restrict__ koff, const double* __restrict__ x,
                            const double* __restrict__ y, const double* __restrict__ z, int dim, double inv2s2_all,
                            const double* __restrict__ cell_sig, double shift, T* __restrict__ K,
-                           const unsigned char* __restrict__ only, const float2* __restrict__ hl, long long n) {
+                           const unsigned char* __restrict__ only, const float2* __restrict__ hl, long long n,
+                           double kexp_all, const double* __restrict__ tab) {
   int b = blockIdx.y;
   if (b >= nblk || (only && !only[b])) return;
   int c = blk_cell[b];
   const double inv2s2 = cell_sig ? 1.0 / (2.0 * cell_sig[c] * cell_sig[c]) : inv2s2_all;
+  const double kexp = cell_sig ? kexp_of_sigma(cell_sig[c]) : kexp_all;
   int nbk = (int)(boff[c + 1] - boff[c]);
   int nc = cs[c + 1] - cs[c], n1 = nbk - nc;
   const int* id = idx + boff[c];
@@ -146,14 +164,14 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
         if (i == j) v += (float)shift;
         A[(long long)i * nbk + j] = v;
       } else {
-        double dx = xa - x[pb], dy = ya - y[pb];
-        double r2 = dx * dx + dy * dy;
+        const double dx = __dsub_rn(xa, x[pb]), dy = __dsub_rn(ya, y[pb]);
+        double r2 = __fma_rn(dy, dy, __dmul_rn(dx, dx));
         if (dim == 3) {
-          double dz = za - z[pb];
-          r2 += dz * dz;
+          const double dz = __dsub_rn(za, z[pb]);
+          r2 = __fma_rn(dz, dz, r2);
         }
-        double v = exp(-r2 * inv2s2);
-        if (i == j) v += shift;
+        double v = exp_neg_tab(r2, kexp, tab);
+        if (i == j) v = __dadd_rn(v, shift);
         A[(long long)i * nbk + j] = v;
       }
     }
@@ -367,6 +385,94 @@ __device__ bool potrf_trtri(T* C, T* M, int h) {
   }
   __syncthreads();
   return s_bad == 0;
+}
+
+// Ordered form of the diagonal-tile Cholesky (plain FP64 factor form): the h x h leading
+// part of C (lower) becomes L_kk in place, rd[j] = 1 / L_kk[j][j]. Column j: s = sqrt(c_jj),
+// r = 1/s, l_ij = c_ij * r, then c_il = fma(-l_ij, l_lj, c_il) for j < l <= i. Every entry
+// thus receives its updates in ascending column order, each one rounding, exactly as the
+// unblocked right-looking Cholesky with those operations computes it. Returns false if a
+// pivot is not positive (it is then taken as 1 and the block retried with a shift).
+// Entries outside h x h are set to the identity.
+template <class T>
+__device__ bool potrf_rd(T* C, T* rd, int h) {
+  constexpr int S = SP<T>::S;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < TB * TB; e += NTH) {
+    int r = e / TB, c = e % TB;
+    if (r >= h || c >= h) C[r * S + c] = (r == c) ? T(1) : T(0);
+    if (c > r) C[r * S + c] = T(0);
+  }
+  __syncthreads();
+  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  for (int j = 0; j < h; j++) {
+    T d = C[j * S + j];
+    if (!(d > T(0))) {
+      if (threadIdx.x == 0) s_bad = 1;
+      d = T(1);
+    }
+    const T sq = sqrt(d);
+    const T rc = T(1) / sq;
+    __syncthreads();
+    for (int i = j + 1 + threadIdx.x; i < h; i += NTH) C[i * S + j] = C[i * S + j] * rc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      C[j * S + j] = sq;
+      rd[j] = rc;
+    }
+    T ci[4], cl[4];
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+      const int i = 4 * ty + p, l = 4 * tx + p;
+      ci[p] = (i > j && i < h) ? C[i * S + j] : T(0);
+      cl[p] = (l > j && l < h) ? C[l * S + j] : T(0);
+    }
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int i = 4 * ty + p, l = 4 * tx + q;
+        if (l > j && l <= i && i < h) C[i * S + l] = fma(-ci[p], cl[q], C[i * S + l]);
+      }
+    __syncthreads();
+  }
+  for (int j = h + threadIdx.x; j < TB; j += NTH) rd[j] = T(1);
+  __syncthreads();
+  return s_bad == 0;
+}
+
+// Panel solve of the ordered factor form: rows of C (a tile below the diagonal, after its
+// trailing updates) become C L_kk^-T in place: for k = 0 .. hk-1, l_rk = c_rk * rd[k], then
+// c_rj = fma(-l_rk, L_kk[j][k], c_rj) for k < j < hk -- per entry the same sequence as the
+// unblocked algorithm, with no explicit inverse. Four threads per row, thread sub owning
+// columns sub + 4m (register-resident; k is unrolled so every index is static); the pivot
+// column's owner scales and broadcasts within its quad. Rows at or past hi are zero padding
+// (whole warps beyond them return). All threads of a warp reach every shuffle.
+template <class T>
+__device__ void trsm_rows(T* C, const T* Lk, const T* rd, int hi, int hk) {
+  constexpr int S = SP<T>::S;
+  static_assert(TB == 64 && NTH == 256, "64 rows x 4 threads");
+  const int r = threadIdx.x >> 2, sub = threadIdx.x & 3, lane = threadIdx.x & 31;
+  if ((r & ~7) >= hi) return;  // warp-uniform: every row of this warp is padding
+  T c[16];
+#pragma unroll
+  for (int m = 0; m < 16; m++) c[m] = C[r * S + sub + 4 * m];
+  const T* lrow = Lk + sub * S;  // row sub + 4m of L_kk at lrow[4 m S] (static offsets)
+#pragma unroll
+  for (int k = 0; k < TB; k++) {
+    if (k >= hk) break;
+    const int owner = k & 3, m0 = k >> 2;
+    T x = c[m0] * rd[k];
+    x = __shfl_sync(0xffffffffu, x, (lane & ~3) | owner);
+    if (sub == owner) c[m0] = x;
+    if (sub > owner) c[m0] = fma(-x, lrow[4 * m0 * S + k], c[m0]);
+#pragma unroll
+    for (int m = m0 + 1; m < 16; m++) c[m] = fma(-x, lrow[4 * m * S + k], c[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < 16; m++) C[r * S + sub + 4 * m] = c[m];
 }
 
 template <class T>
@@ -880,6 +986,89 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
   if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
 }
 
+// ---- plain FP64 factor form: ordered block Cholesky -----------------------------------
+// One CTA per block: left-looking Cholesky of K over uniform 64 x 64 tiles. A tile starts
+// from K, receives the trailing updates of the earlier tile columns in ascending column
+// order (tile_update accumulates into the tile itself), and is then finished by potrf_rd
+// (diagonal tile) or trsm_rows (tiles below it). Every entry of L thus sees exactly the
+// operation sequence of the unblocked right-looking Cholesky written with fma, sqrt and
+// reciprocal pivots -- a CPU restatement of that loop reproduces the factor bit for bit.
+// The factor is then packed as the apply reads it: row i holds L_A[i][0..i-1] and
+// 1 / L_A[i][i], L_A = L_K sqrt(1 / (2 pi sigma^2)) the factor of A = K / (2 pi sigma^2).
+__global__ void __launch_bounds__(NTH, 2) k_chol_fp64(int nblk, const int* __restrict__ blk_cell,
+                                                   const long long* __restrict__ boff,
+                                                   const long long* __restrict__ koff, double* __restrict__ K,
+                                                   double out_scale_all, const double* __restrict__ cell_sig,
+                                                   unsigned char* __restrict__ bad,
+                                                   const unsigned char* __restrict__ only,
+                                                   const long long* __restrict__ loff, double* __restrict__ Lpack) {
+  using T = double;
+  const int b = blockIdx.x;
+  if (b >= nblk || (only && !only[b])) return;
+  double out_scale = out_scale_all;  // sqrt(1 / (2 pi sigma^2)), per cell for a batch
+  if (cell_sig) {
+    const double sg = cell_sig[blk_cell[b]];
+    out_scale = sqrt(1.0 / (2.0 * M_PI * sg * sg));
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T s_rd[TB];
+  constexpr int S = SP<T>::S;
+  constexpr int KC = KCOf<T>::v;
+  Tiles<T> t;
+  t.As = (T*)smem_raw;
+  t.Bs = t.As + 2 * KC * S;
+  t.C = t.Bs + 2 * KC * S;
+  t.M = t.C + TB * S;
+  const int c = blk_cell[b];
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  const int ntile = (nb + TB - 1) / TB;
+  T* A = K + koff[b];
+  bool ok = true;
+  for (int k = 0; k < ntile; k++) {
+    const int rk = k * TB, hk = min(TB, nb - rk);
+    for (int i = k; i < ntile; i++) {
+      const int ri = i * TB, hi = min(TB, nb - ri);
+      T acc[4][4];
+      load_acc<T>(A, nb, ri, rk, hi, hk, acc, true);
+      for (int p = 0; p < k; p++) {
+        const int rp = p * TB, hp = min(TB, nb - rp);
+        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, A, nb, rk, rp, hk, false, hp);
+      }
+      __syncthreads();
+      acc_to_smem<T>(t.C, acc);
+      __syncthreads();
+      if (i == k) {
+        ok = potrf_rd<T>(t.C, s_rd, hk) && ok;
+        // store L_kk and keep it in M for the panel solves of this tile column
+        for (int e = threadIdx.x; e < TB * TB; e += NTH) {
+          const int r = e / TB, cc = e % TB;
+          const T v = t.C[r * S + cc];
+          if (r < hk && cc <= r) A[(long long)(rk + r) * nb + rk + cc] = v;
+          t.M[r * S + cc] = v;
+        }
+      } else {
+        trsm_rows<T>(t.C, t.M, s_rd, hi, hk);
+        __syncthreads();
+        for (int e = threadIdx.x; e < TB * TB; e += NTH) {
+          const int r = e / TB, cc = e % TB;
+          if (r < hi && cc < hk) A[(long long)(ri + r) * nb + rk + cc] = t.C[r * S + cc];
+        }
+      }
+      __syncthreads();
+    }
+  }
+  T* Lp = Lpack + loff[c];
+  const T sc = (T)out_scale;
+  for (int i = 0; i < nb; i++) {
+    const long long o = rowoff<T>(i);
+    for (int j = threadIdx.x; j <= i; j += NTH) {
+      const T v = A[(long long)i * nb + j] * sc;
+      Lp[o + j] = j == i ? T(1) / v : v;
+    }
+  }
+  if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
+}
+
 // ---- apply: out[centre(c)] = S_c r[buffer(c) in block order] --------------------------
 template <class T>
 __global__ void __launch_bounds__(128) k_apply(int ncell, const long long* __restrict__ boff,
@@ -1161,6 +1350,36 @@ void rasm_build(RasmPlan& R, const PointSet& P, bool fp32, Workspace& ws, unsign
   rasm_factor(R, G, hcnt, hcs, fp32, ws, err, s, ws_budget_bytes, factor, basic);
 }
 
+void rasm_block_K(const RasmPlan& R, const PointSet& P, int cell, int nb, double* K_dev, Workspace& ws,
+                  cudaStream_t s) {
+  int* dbc = (int*)ws.get(41, sizeof(int));
+  long long* dk = (long long*)ws.get(42, sizeof(long long) * 2);
+  const long long hk[2] = {0, (long long)nb * nb};
+  PRBF_CUDA(cudaMemcpyAsync(dbc, &cell, sizeof(int), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyAsync(dk, hk, sizeof(hk), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemsetAsync(K_dev, 0, sizeof(double) * (size_t)nb * nb, s));
+  const Grid& g = P.g;
+  k_assemble<double><<<dim3(64, 1), 256, 0, s>>>(1, dbc, R.boff.get(), P.cs.get(), R.idx.get(), dk, P.x.get(),
+                                                  P.y.get(), P.view().z, g.dim, 1.0 / (2.0 * g.sigma * g.sigma),
+                                                  nullptr, 0.0, K_dev, nullptr, nullptr, 0, kexp_of_sigma(g.sigma),
+                                                  exp_table_dev(s));
+  PRBF_CHECK_LAUNCH();
+  PRBF_CUDA(cudaStreamSynchronize(s));  // the host copies of dbc / dk stay valid until here
+}
+
+void rasm_factor_rows(const RasmPlan& R, int cell, int nb, double* out, cudaStream_t s) {
+  if (!R.factor || R.fp32) throw Error(PRBF_ERR_STATE, "the plan keeps no FP64 factor");
+  long long lo[2];
+  PRBF_CUDA(cudaMemcpyAsync(lo, R.loff.get() + cell, sizeof(lo), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  if (lo[1] - lo[0] != rowoff<double>(nb)) throw Error(PRBF_ERR_STATE, "factor size does not match the block");
+  std::vector<double> h((size_t)(lo[1] - lo[0]));
+  PRBF_CUDA(cudaMemcpyAsync(h.data(), R.L64.get() + lo[0], sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  for (long long i = 0; i < nb; i++)
+    std::copy(h.begin() + rowoff<double>(i), h.begin() + rowoff<double>(i) + i + 1, out + i * (i + 1) / 2);
+}
+
 void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff_dev, int* idx_dev, cudaStream_t s) {
   const Grid& g = P.g;
   k_buffer_lists<<<ceil_div(g.ncell, 8), 256, 0, s>>>(g, P.x.get(), P.y.get(), P.view().z, P.cs.get(),
@@ -1244,7 +1463,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_tc_smem()));
   } else
-    PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PRBF_CUDA(cudaFuncSetAttribute(k_chol_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   R.nfallback = 0;
   R.retried.clear();
   // FP32 form: the coordinates split into float pairs once (the assembly then stays on the
@@ -1297,7 +1516,8 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       dim3 ag(64, nb_batch);
       if (fp32) {
         k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
-                                             inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n);
+                                             inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n,
+                                             0.0, nullptr);
         PRBF_CHECK_LAUNCH();
         // the Cholesky on the tensor cores, then the factor / S_c epilogues of k_chol_sc
         k_chol_tc<<<nb_batch, NTH, chol_tc_smem(), s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
@@ -1313,12 +1533,12 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
                                                        G.cell_sigma, dbad, only, 0, nullptr, nullptr, 1);
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
-                                              G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only, nullptr, 0);
+                                              G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only, nullptr, 0,
+                                              kexp_of_sigma(G.sigma), exp_table_dev(s));
         PRBF_CHECK_LAUNCH();
-        k_chol_sc<double><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (double*)Kw, dx,
-                                                      (double*)Xw, R.soff.get(), nullptr,
-                                                      std::sqrt(1.0 / out_scale), G.cell_sigma, dbad, only, 1,
-                                                      R.loff.get(), R.L64.get(), 0);
+        k_chol_fp64<<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), dk, (double*)Kw,
+                                                std::sqrt(1.0 / out_scale), G.cell_sigma, dbad, only, R.loff.get(),
+                                                R.L64.get());
       }
       PRBF_CHECK_LAUNCH();
       hbad.resize(nb_batch);

@@ -54,6 +54,14 @@ void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff
 // indices) and their host sizes: hcnt[c] block sizes, hcs the cell starts.
 void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, const std::vector<int>& hcs, bool fp32,
                  Workspace& ws, unsigned* err, cudaStream_t s, double ws_budget_bytes, bool factor, bool basic);
+// K = 2 pi sigma^2 A_c of one block of a single-problem plan, as the FP64 factorisation
+// assembles it (rows neighbours first, lower triangle, no diagonal shift), into K_dev
+// (nb x nb, zeroed first). Synchronises the stream.
+void rasm_block_K(const RasmPlan& R, const PointSet& P, int cell, int nb, double* K_dev, Workspace& ws,
+                  cudaStream_t s);
+// The FP64 factor of one block as stored (row i: L_A[i][0..i-1] then 1/L_A[i][i]), the
+// rows' padding removed, into out (host, nb (nb + 1) / 2 entries).
+void rasm_factor_rows(const RasmPlan& R, int cell, int nb, double* out, cudaStream_t s);
 // Sets the dynamic shared memory limit of the apply kernel for this plan.
 void rasm_set_apply_smem(const RasmPlan& R);
 // Restricted: out[centre(c)] = (A_c^-1 r[buffer(c)])[centre] for every cell; basic:

@@ -387,6 +387,50 @@ int prbf_pc_apply(prbf_ctx* ctx, const double* r, double* z) {
   });
 }
 
+int prbf_pc_buffer_lists(prbf_ctx* ctx, long long* off_out, int* idx_out) {
+  return ctx_call(ctx, [&](Ctx& c) {
+    if (!c.solve || !c.solve->pc_ready) throw Error(PRBF_ERR_STATE, "prbf_pc_setup has not been called");
+    const RasmPlan& R = c.solve->pc;
+    const int ncell = c.mv_pts.g.ncell;
+    std::vector<long long> off(ncell + 1);
+    PRBF_CUDA(cudaMemcpyAsync(off.data(), R.boff.get(), sizeof(long long) * (ncell + 1), cudaMemcpyDeviceToHost,
+                              c.stream));
+    PRBF_CUDA(cudaStreamSynchronize(c.stream));
+    if (off_out) std::copy(off.begin(), off.end(), off_out);
+    if (idx_out && off[ncell] > 0) {
+      PRBF_CUDA(cudaMemcpyAsync(idx_out, R.idx.get(), sizeof(int) * off[ncell], cudaMemcpyDeviceToHost, c.stream));
+      PRBF_CUDA(cudaStreamSynchronize(c.stream));
+    }
+  });
+}
+
+int prbf_pc_block(prbf_ctx* ctx, int cell, int* nb_out, int* nc_out, double* K_out, double* L_out) {
+  return ctx_call(ctx, [&](Ctx& c) {
+    if (!c.solve || !c.solve->pc_ready) throw Error(PRBF_ERR_STATE, "prbf_pc_setup has not been called");
+    const RasmPlan& R = c.solve->pc;
+    if (cell < 0 || cell >= c.mv_pts.g.ncell) throw Error(PRBF_ERR_ARG, "no such cell");
+    long long bo[2];
+    int cs2[2];
+    PRBF_CUDA(cudaMemcpyAsync(bo, R.boff.get() + cell, sizeof(bo), cudaMemcpyDeviceToHost, c.stream));
+    PRBF_CUDA(cudaMemcpyAsync(cs2, c.mv_pts.cs.get() + cell, sizeof(cs2), cudaMemcpyDeviceToHost, c.stream));
+    PRBF_CUDA(cudaStreamSynchronize(c.stream));
+    const int nb = (int)(bo[1] - bo[0]), nc = cs2[1] - cs2[0];
+    if (nb_out) *nb_out = nb;
+    if (nc_out) *nc_out = nc;
+    if (nb == 0) return;
+    if (K_out) {
+      double* Kd = (double*)c.ws.get(56, sizeof(double) * (size_t)nb * nb);
+      rasm_block_K(R, c.mv_pts, cell, nb, Kd, c.ws, c.stream);
+      PRBF_CUDA(cudaMemcpyAsync(K_out, Kd, sizeof(double) * (size_t)nb * nb, cudaMemcpyDeviceToHost, c.stream));
+      PRBF_CUDA(cudaStreamSynchronize(c.stream));
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < i; j++) K_out[(size_t)j * nb + i] = K_out[(size_t)i * nb + j];
+      c.check_device_error("block read-back");
+    }
+    if (L_out) rasm_factor_rows(R, cell, nb, L_out, c.stream);
+  });
+}
+
 // 3d/wrapper.cxx:20-105 with the same argument meaning. It creates its own context on
 // device 0 (the reference calls PetscInitialize on every call) and frees it on return.
 int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, float* zg, float* wg, int np, float* xp,
@@ -423,3 +467,12 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
 }
 
 }  // extern "C"
+
+// The reference's library entry with its own C++ signature and linkage (3d/wrapper.cxx:20-23,
+// the symbol librbf.a exports), so a program built against librbf.a links against this
+// library unchanged.
+int RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, float* zg, float* wg, int np, float* xp,
+                     float* yp, float* zp, float* gp, float sigma, int nsigma_box, int sigma_buffer, int sigma_trunc) {
+  return prbf_RBFInterpolation(argc, argv, ng, xg, yg, zg, wg, np, xp, yp, zp, gp, sigma, nsigma_box, sigma_buffer,
+                               sigma_trunc);
+}

@@ -12,9 +12,12 @@ pytestmark = pytest.mark.gpu
 # Solved weights, plain FP64 vs the oracle (relative 2-norm), for solves run to
 # convergence (rtol 1e-16): both reach the same discrete solution.
 RTOL_WEIGHTS = 1e-10
-# At the reference's stopping rule (rtol 1e-13 on the preconditioned residual) GMRES
-# stops before the weights settle: the oracle's own 1e-13 solution differs from its
-# converged one by 1.5e-10 on the 10^4-point lattice, so two implementations agree to a few 1e-10.
+# The weights' rounding floor on the 10^4-point lattice: the oracle against itself with
+# only the summation order of its matvec rows reversed stops after the same iterations with
+# weights 1.8e-10 apart, converged or at the reference's rtol 1e-13
+# (test_oracle.py::test_weights_move_with_rounding_order_alone). The GPU's pair sums round
+# differently from the oracle's row sums, so at that stopping rule the solves are compared
+# with equal iteration counts and this envelope.
 RTOL_WEIGHTS_AT_1E13 = 5e-10
 
 
@@ -48,14 +51,19 @@ def test_rasm_apply_matches_oracle(jitter):
     R = O.Rasm(g, p.x[perm], p.y[perm], None, cs)
     ref = np.empty(p.n)
     ref[perm] = R.apply(r[perm])
+    Rc = O.Rasm(g, p.x[perm], p.y[perm], None, cs, factor="chol")
+    refc = np.empty(p.n)
+    refc[perm] = Rc.apply(r[perm])
     with _ctx(p) as c:
         c.matvec_setup(p.x, p.y)
         c.pc_setup("fp64")
         z64 = c.pc_apply(r)
         c.pc_setup("mixed")
         z32 = c.pc_apply(r)
-    # Cholesky (GPU) vs partial-pivoting LU (oracle) of the same SPD blocks: both are
-    # backward stable, so they agree to about cond(A_c) * eps
+    # bit for bit against the oracle's restatement of the GPU's block arithmetic
+    np.testing.assert_array_equal(z64, refc)
+    # Cholesky (GPU) vs partial-pivoting LU (oracle, the reference's) of the same SPD
+    # blocks: both are backward stable, so they agree to about cond(A_c) * eps
     assert _rel(z64, ref) < 1e-7
     assert _rel(z32, ref) < 0.2  # FP32 factors: a preconditioner, not a solve
 
@@ -88,12 +96,29 @@ def test_true_residual_solve_matches_oracle_converged():
     assert abs(_offgrid_err(p, g) - _offgrid_err(p, go)) < 1e-3
 
 
+@pytest.mark.parametrize("case", ["lattice100", "jitter50", "jitter100"])
+def test_solve_at_reference_stop_matches_oracle(case):
+    """At the reference's stopping rule the GPU takes exactly the oracle's iterations, with
+    the reference's LU blocks and with the GPU's own block arithmetic restated, and its
+    weights lie within the rounding floor of both."""
+    p = {"lattice100": W.lamb_oseen_lattice_1e4,
+         "jitter50": lambda: W.lamb_oseen_2d(50, jitter=0.25, seed=8),
+         "jitter100": lambda: W.lamb_oseen_2d(100, jitter=0.25, seed=3)}[case]()
+    with _ctx(p) as c:
+        g, st = c.interpolate(p.x, p.y, None, p.f)
+    assert st.reason == 2
+    for factor in ("lu", "chol"):
+        go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), factor=factor)
+        assert reason_o == 2 and st.its == its_o
+        assert _rel(g, go) <= RTOL_WEIGHTS_AT_1E13
+
+
 def test_solve_lamb_oseen_lattice_1e4_fp64_matches_oracle():
     p = W.lamb_oseen_lattice_1e4()
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params())
     with _ctx(p) as c:
         g, st = c.interpolate(p.x, p.y, None, p.f)
-    assert st.reason == 2 and abs(st.its - its_o) <= 2
+    assert st.reason == 2 and st.its == its_o
     assert st.true_rel_resid < 1e-11
     assert _rel(g, go) <= RTOL_WEIGHTS_AT_1E13
     # At the collocation points the error metric of 2d/main.cxx:130-133 equals the true
@@ -231,7 +256,7 @@ def test_basic_asm_solve_3d_matches_oracle():
                      max_it=400) as c:
             g, st = c.interpolate(x, y, z, wx)
         assert reason_o == 2 and st.reason == 2
-        assert abs(st.its - its_o) <= 1
+        assert st.its == its_o
         assert _rel(g, go) <= RTOL_WEIGHTS
 
 
@@ -317,7 +342,7 @@ def test_cdata_cylinder_matches_oracle(golden):
     with _ctx(p, rtol=1e-13, max_it=1000) as c:
         g, st = c.interpolate(p.x, p.y, None, p.f)
         w = c.evaluate(p.x, p.y, None, p.x, p.y, None, g)
-    assert st.reason == 2 and abs(st.its - int(d["solve_its"][0])) <= 2
+    assert st.reason == 2 and st.its == int(d["solve_its"][0])
     assert _rel(g, d["solve_weights"]) <= RTOL_WEIGHTS_AT_1E13
     # error metric of the cylinder driver (2d/cylinder.cxx:123-127): residual level
     err = W.log10_rel_error(w, p.f)
@@ -330,7 +355,9 @@ def test_edge_point_sets(precision):
     # one point: g = f 2 pi sigma^2
     with Context(sigma=0.025, **kw) as c:
         g, st = c.interpolate(np.array([0.3]), np.array([-0.2]), None, np.array([1.5]))
-    assert st.reason == 2 and abs(g[0] - 1.5 * 2 * np.pi * 0.025 ** 2) <= 1e-13 * g[0]
+    # the one-point block solve is exact, so the first residual can be exactly zero
+    # (PETSc's KSP_CONVERGED_ATOL, reason 3)
+    assert st.reason in (2, 3) and abs(g[0] - 1.5 * 2 * np.pi * 0.025 ** 2) <= 1e-13 * g[0]
     # collinear points (a degenerate bounding box: one row of cells)
     xl = np.linspace(-1, 1, 1000)
     with Context(sigma=2.0 / 999 / 0.8, **kw) as c:
@@ -353,4 +380,4 @@ def test_edge_point_sets(precision):
     with _ctx(p, precision=precision, max_it=200) as c:
         with pytest.raises(PrbfError) as e:
             c.interpolate(x, y, None, f2)
-    assert e.value.status == 5  # PRBF_ERR_NOT_CONVERGED
+    assert e.value.status in (5, 10)  # PRBF_ERR_NOT_CONVERGED, or PRBF_ERR_DIVERGED (past dtol)

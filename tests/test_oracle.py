@@ -195,3 +195,69 @@ def test_cdata_cylinder_solve_reproduces_fixture(golden):
     np.testing.assert_allclose(gw, d["solve_weights"], rtol=0, atol=1e-12 * np.abs(d["solve_weights"]).max())
     w = O.vorticity_evaluation(p.x, p.y, None, p.x, p.y, None, gw, *p.params())
     assert abs(W.log10_rel_error(w, p.f) - float(d["solve_log10_err"][0])) < 1e-6
+
+
+def test_cholesky_restatement_against_dense_solves():
+    # the GPU library's block arithmetic restated (factor "chol"): blocks in its order
+    # (neighbours first), its table exp; restricted and basic applies against dense solves
+    x, y, z, h = W.lattice_3d(8, jitter=0.25, seed=6)
+    prm = (h / 0.8, 2, 6, 16)
+    g = O.grid_for(x, y, z, *prm)
+    perm, cs = O.cell_sort(g, x, y, z)
+    xs, ys, zs = x[perm], y[perm], z[perm]
+    off, idx = O.buffer_lists(g, xs, ys, zs, cs)
+    r = np.random.default_rng(8).standard_normal(len(x))
+    for basic in (False, True):
+        R = O.Rasm(g, xs, ys, zs, cs, basic=basic, factor="chol")
+        assert R.status == 0
+        out = R.apply(r)
+        ref = np.zeros(len(x))
+        for c in range(g.ncell):
+            b = idx[off[c]:off[c + 1]]
+            if not len(b):
+                continue
+            nc = cs[c + 1] - cs[c]
+            K = O.gpu_block(g, b, nc, xs, ys, zs)
+            order = np.r_[np.arange(nc, len(b)), np.arange(nc)]
+            # the table exp agrees with libm's to the rounding of the exponent argument
+            A = O.block(g, b, xs, ys, zs)[np.ix_(order, order)]
+            assert np.abs(K / (2 * np.pi * prm[0] ** 2) - A).max() <= 1e-13 * np.abs(A).max()
+            sol = sla.solve(K, r[b][order], assume_a="pos") * (2 * np.pi * prm[0] ** 2)
+            if basic:
+                ref[b[order]] += sol
+            else:
+                ref[cs[c]:cs[c + 1]] = sol[len(b) - nc:]
+        assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-9
+        # the packed factor reproduces the block: L L^T = A (block order)
+        c = int(np.argmax(np.diff(off)))
+        nb, nc, _ = R.block_info(c)
+        rows = R.factor_rows(c)
+        L = np.zeros((nb, nb))
+        for i in range(nb):
+            L[i, :i + 1] = rows[i * (i + 1) // 2:(i + 1) * (i + 2) // 2]
+            L[i, i] = 1.0 / L[i, i]
+        K = O.gpu_block(g, idx[off[c]:off[c + 1]], nc, xs, ys, zs) / (2 * np.pi * prm[0] ** 2)
+        assert np.abs(L @ L.T - K).max() <= 1e-13 * np.abs(K).max()
+
+
+def test_weights_move_with_rounding_order_alone():
+    """The rounding floor of the solved weights on the 10^4-point lattice. The same oracle
+    with each matvec row's terms summed last-to-first -- the same operator, another
+    rounding order -- stops after the same 11 iterations at the reference's rule (rtol 1e-13
+    on the preconditioned residual) with weights 1.8e-10 away, and run to convergence
+    (rtol 1e-16) the two discrete solutions are still 1.8e-10 apart: the weights' forward
+    error under a last-bit change of the operator. Two implementations whose sums round
+    differently (a CPU row sum and a GPU pair sum) cannot agree more closely than this;
+    they are compared with equal iteration counts and this envelope."""
+    p = W.lamb_oseen_lattice_1e4()
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    g1, its1, r1 = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), factor="chol")
+    g2, its2, r2 = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), factor="chol", reverse_sums=True)
+    assert r1 == r2 == 2 and its1 == its2
+    assert 2e-11 < rel(g2, g1) < 5e-10
+    gc1, _, q1 = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), factor="chol", rtol=1e-16, max_it=60)
+    gc2, _, q2 = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), factor="chol", rtol=1e-16, max_it=60,
+                                     reverse_sums=True)
+    assert q1 == q2 == 2
+    assert 2e-11 < rel(gc2, gc1) < 5e-10
+    assert rel(g1, gc1) < 1e-12  # the same arithmetic: its 1e-13 stop is already at its solution
