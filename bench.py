@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--nprob", type=int, default=256, help="problems (batch2d)")
     ap.add_argument("--batch-max-it", type=int, default=1000)
     ap.add_argument("--case", default=None, help="run one small kernel case (ncu captures) and exit")
+    ap.add_argument("--sections", default="solve,cpu_solve,cpu_solve_4e6,vortex3d,batch2d,learned",
+                    help="extra sections of the default line after the timed steps (comma list)")
+    ap.add_argument("--cpu-solve-child", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--seed", type=int, default=12345, help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -348,22 +352,31 @@ def run_ours(args, rank, world):
     }
     if rank == 0 and world == 1:
         result["cpu_baseline"] = cpu_baseline()
-    if not args.skip_solve:
-        result["solve"] = solve_section(p, dev, rank)
-        if rank == 0 and world == 1:
-            result["cpu_solve"] = cpu_solve_section(p, dev, pairs, result["solve"]["fp64"])
+    sections = set() if args.skip_solve else set(args.sections.split(","))
+    if "solve" in sections:
+        result["solve"], g64 = solve_section(p, dev, rank)
+        if rank == 0 and world == 1 and "cpu_solve" in sections:
+            result["cpu_solve"] = cpu_solve_section(dev)
+            if "cpu_solve_4e6" in sections:
+                result["cpu_solve"]["lamb_oseen_jitter_4e6"] = cpu_solve_full(p, args, g64, result["solve"]["fp64"])
+    if rank == 0 and world == 1:
+        if "vortex3d" in sections:
+            result["vortex3d"] = vortex3d_section(args.m3)
+        if "batch2d" in sections:
+            result["batch2d"] = batch2d_section(args.nprob, args.batch_max_it)
+        if "learned" in sections:
+            result["learned_heldout"] = learned_heldout_section(dev)
     if rank == 0:
         print(json.dumps(result), flush=True)
 
 
-def cpu_solve_section(p2, dev, pairs2, gpu2):
-    """The solve on the host cores beside the GPU: the 10^4-point 100 x 100 lattice solved
-    to 1e-13 by the oracle (the C++ restatement of the reference's solve: cell list, dense
-    Schwarz blocks, GMRES(30); OpenMP over cells) and by the plain FP64 GPU form, and the
-    oracle's time for the 4x10^6-point problem p2 extrapolated from the small solve's rates:
-    block set-up by the sum of n_b^3, Schwarz applies by the sum of n_b^2, matvecs by the
-    pairs, with p2's GPU iteration count (a full CPU solve of p2 takes far longer than a
-    bench run)."""
+def cpu_solve_section(dev):
+    """The 10^4-point 100 x 100 lattice (config 1) solved to 1e-13 on the host cores by the
+    oracle -- the C++ restatement of the reference's solve (cell list, dense Schwarz blocks
+    with PETSc's LU, GMRES(30); OpenMP over cells), and the same with the GPU library's
+    block arithmetic restated (Cholesky) -- and by the plain FP64 GPU form: times,
+    iterations, and the weights' distance, beside the oracle's own rounding floor (the same
+    solve with every matvec row summed in reverse order)."""
     import oracle as O
     from petrbf_gb300 import workloads as W
     from petrbf_gb300.api import Context
@@ -374,56 +387,109 @@ def cpu_solve_section(p2, dev, pairs2, gpu2):
         c.interpolate(p.x, p.y, None, p.f)  # first call: allocations and graph capture
         g_gpu, st = c.interpolate(p.x, p.y, None, p.f)
     gpu_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out = {"cores": O.num_threads(), "kind": "port"}
+    row = {"workload": p.name, "n_points": p.n, "gpu_time_s": gpu_s, "gpu_its": st.its,
+           "gpu_pts_per_s": p.n / gpu_s}
+    sols = {}
+    for factor in ("lu", "chol"):
+        t0 = time.perf_counter()
+        g = O.grid_for(p.x, p.y, None, *prm)
+        perm, cs = O.cell_sort(g, p.x, p.y)
+        xs, ys = p.x[perm], p.y[perm]
+        t1 = time.perf_counter()
+        R = O.Rasm(g, xs, ys, None, cs, factor=factor)
+        t2 = time.perf_counter()
+        sol, its, reason, _ = O.gmres(g, xs, ys, None, cs, R, p.f[perm])
+        t3 = time.perf_counter()
+        R.close()
+        gc = np.empty_like(sol)
+        gc[perm] = sol
+        sols[factor] = gc
+        row["cpu_" + factor] = {"time_s": t3 - t0, "setup_s": t2 - t1, "gmres_s": t3 - t2, "its": its,
+                                "reason": reason, "pts_per_s": p.n / (t3 - t0),
+                                "weights_rel_diff_gpu_vs_cpu": rel(g_gpu, gc)}
+    g_rev, its_rev, _ = O.rbf_interpolation(p.x, p.y, None, p.f, *prm, factor="chol", reverse_sums=True)
+    row["oracle_rounding_floor"] = {"its": its_rev, "weights_rel_diff": rel(g_rev, sols["chol"]),
+                                    "what": "the chol oracle against itself with every matvec row summed in "
+                                            "reverse order (same operator, another rounding)"}
+    row["note"] = ("cpu_lu is the reference's algorithm (PETSc LU blocks); cpu_chol restates the GPU library's "
+                   "block arithmetic, so its Schwarz applies are bit-identical to the GPU's")
+    out["lamb_oseen_lattice_1e4"] = row
+    return out
+
+
+def _meminfo_available():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def cpu_solve_child(args):
+    """(child process) The 4x10^6-point problem solved to 1e-13 by the oracle on all host
+    cores, with the GPU library's block arithmetic restated (packed FP64 Cholesky factors
+    of the 40,000 blocks, ~127 GB). The address space is capped before the factors are
+    allocated, so exhausting it fails this process, not the machine."""
+    import resource
+    import oracle as O
+    from petrbf_gb300 import workloads as W
+    p = W.lamb_oseen_2d(args.m, jitter=0.25, seed=args.seed)
+    res = {"status": "ok"}
     t0 = time.perf_counter()
-    g = O.grid_for(p.x, p.y, None, *prm)
+    g = O.grid_for(p.x, p.y, None, *p.params())
     perm, cs = O.cell_sort(g, p.x, p.y)
     xs, ys = p.x[perm], p.y[perm]
-    t1 = time.perf_counter()
-    R = O.Rasm(g, xs, ys, None, cs)
-    t2 = time.perf_counter()
-    sol, its, reason, _ = O.gmres(g, xs, ys, None, cs, R, p.f[perm])
-    t3 = time.perf_counter()
-    g_cpu = np.empty_like(sol)
-    g_cpu[perm] = sol
-    v = np.random.default_rng(3).standard_normal(p.n)
-    reps = 5
-    ta = time.perf_counter()
-    for _ in range(reps):
-        R.apply(v)
-    t_apply = (time.perf_counter() - ta) / reps
-    tm = time.perf_counter()
-    for _ in range(reps):
-        O.matvec(g, xs, ys, None, cs, v)
-    t_mv = (time.perf_counter() - tm) / reps
-    R.close()
-    pairs1 = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
-    nb1 = O.buffer_counts(g, xs, ys, None, cs).astype(np.float64)
-    # p2's blocks, from its own cell list
-    g2 = O.grid_for(p2.x, p2.y, None, *p2.params())
-    perm2, cs2 = O.cell_sort(g2, p2.x, p2.y)
-    nb2 = O.buffer_counts(g2, p2.x[perm2], p2.y[perm2], None, cs2).astype(np.float64)
-    r3, r2 = (nb2 ** 3).sum() / (nb1 ** 3).sum(), (nb2 ** 2).sum() / (nb1 ** 2).sum()
-    its2 = gpu2["its"]
-    setup2 = (t2 - t1) * r3
-    iter2 = (its2 + 1) * (t_apply * r2 + t_mv * pairs2 / pairs1)
-    cpu2 = setup2 + iter2
-    rel = float(np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu))
-    return {
-        "cores": O.num_threads(), "kind": "port",
-        "lamb_oseen_lattice_1e4": {"workload": p.name, "n_points": p.n,
-                    "cpu_time_s": t3 - t0, "cpu_setup_s": t2 - t1, "cpu_gmres_s": t3 - t2, "cpu_its": its,
-                    "cpu_reason": reason, "gpu_time_s": gpu_s, "gpu_its": st.its,
-                    "weights_rel_diff_gpu_vs_cpu": rel,
-                    "weights_note": "both stop at rtol 1e-13 on the preconditioned residual, before the weights "
-                                    "settle; solved to rtol 1e-16 they agree within 1e-10 (tests)",
-                    "cpu_pts_per_s": p.n / (t3 - t0),
-                    "gpu_pts_per_s": p.n / gpu_s},
-        "lamb_oseen_jitter_4e6_extrapolated": {"cpu_time_s": cpu2, "cpu_setup_s": setup2, "cpu_iterations_s": iter2,
-                                 "its": its2, "block_flops_ratio": r3, "gpu_fp64_time_s": gpu2["time_s"],
-                                 "cpu_pts_per_s": p2.n / cpu2,
-                                 "basis": "the 10^4-point solve's rates scaled by sum n_b^3 (set-up), sum n_b^2 (applies), "
-                                          "pairs (matvecs); its + 1 applies and matvecs"},
-    }
+    nb = O.buffer_counts(g, xs, ys, None, cs).astype(np.float64)
+    need = float(np.sum(nb * (nb + 1) / 2) * 8 + 31 * p.n * 8 * 2 + 4e9)
+    avail = _meminfo_available()
+    res.update(factor_bytes=float(np.sum(nb * (nb + 1) / 2) * 8), mem_available=avail, mem_needed=need)
+    if need > 0.8 * avail:
+        res["status"] = "skipped: the packed FP64 factors need %.0f GB, %.0f GB available" % (need / 1e9, avail / 1e9)
+    else:
+        lim = int(need + 24e9)
+        resource.setrlimit(resource.RLIMIT_AS, (lim, lim))
+        t1 = time.perf_counter()
+        R = O.Rasm(g, xs, ys, None, cs, factor="chol")
+        t2 = time.perf_counter()
+        sol, its, reason, _ = O.gmres(g, xs, ys, None, cs, R, p.f[perm])
+        t3 = time.perf_counter()
+        R.close()
+        gc = np.empty_like(sol)
+        gc[perm] = sol
+        res.update(time_s=t3 - t0, setup_s=t2 - t1, gmres_s=t3 - t2, its=its, reason=reason, cores=O.num_threads(),
+                   setup_status=R.status)
+        np.save(args.cpu_solve_child + ".g.npy", gc)
+    with open(args.cpu_solve_child, "w") as fh:
+        json.dump(res, fh)
+
+
+def cpu_solve_full(p, args, g_gpu, gpu):
+    """The config-2 problem (4x10^6 points) solved on the host cores in a child process
+    (cpu_solve_child), measured, beside the plain FP64 GPU solve of the same points."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "cpu.json")
+        cmd = [sys.executable, os.path.abspath(__file__), "--cpu-solve-child", out, "--m", str(args.m),
+               "--seed", "12345"]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0 or not os.path.exists(out):
+            return {"status": "failed: rc %d %s" % (r.returncode, (r.stderr or "")[-300:]), "wall_s": wall}
+        res = json.load(open(out))
+        if res.get("status") == "ok":
+            gc = np.load(out + ".g.npy")
+            res["weights_rel_diff_gpu_vs_cpu"] = float(np.linalg.norm(g_gpu - gc) / np.linalg.norm(gc))
+            res["gpu_its"] = gpu["its"]
+            res["gpu_fp64_time_s"] = gpu["time_s"]
+            res["cpu_pts_per_s"] = p.n / res["time_s"]
+            res["kind"] = "port (block arithmetic of the GPU library restated: Cholesky)"
+        res["wall_s"] = wall
+        return res
 
 
 def solve_section(p, dev, rank):
@@ -437,6 +503,7 @@ def solve_section(p, dev, rank):
     variants = [("fp64", "zero"), ("mixed", "zero")]
     if have_model:
         variants += [("mixed", "learned"), ("fp64", "learned")]
+    g64 = None
     for prec, guess in variants:
         with Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
                      precision=prec, guess=guess, device=dev) as c:
@@ -446,6 +513,8 @@ def solve_section(p, dev, rank):
             g, st = c.interpolate(p.x, p.y, None, p.f)
             wall = time.perf_counter() - t0
             err = offgrid_error(c, p, g)
+        if prec == "fp64" and guess == "zero":
+            g64 = g
         dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
         key = prec if guess == "zero" else prec + "+learned"
         out[key] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s,
@@ -459,68 +528,105 @@ def solve_section(p, dev, rank):
     if have_model:
         out["learned_mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed+learned"]["time_s"]
     out["metric"] = "pts/s to 1e-13 residual"
+    return out, g64
+
+
+def vortex3d_section(m3=128, m_oracle=32):
+    """Config 3, the 3D mixed-precision form: an m3^3 jittered lattice (128^3 = 2.1x10^6),
+    three vortex-ring right-hand sides, FP32 matvec + FP32 block Cholesky inside FP64
+    refinement to 1e-12, against the plain FP64 GPU solve of the same problem; and at
+    m_oracle^3 (a size the host cores solve in the run) every component's weights against
+    the FP64 oracle (the reference's LU blocks, basic Schwarz, GMRES to 1e-12)."""
+    import oracle as O
+    from petrbf_gb300 import workloads as W
+    from petrbf_gb300.api import Context
+
+    def solve(p, prec):
+        with Context(dim=3, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+                     sigma_trunc=p.sigma_trunc, precision=prec, rtol=1e-12, pc="asm") as c:
+            t0 = time.perf_counter()
+            g, st = c.interpolate(p.x, p.y, p.z, p.f)
+            wall = time.perf_counter() - t0
+        dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
+        return g, {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s, "its": st.its,
+                   "outer_its": st.outer_its, "reason": st.reason, "true_rel_resid": st.true_rel_resid,
+                   "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms, "t_solve_ms": st.t_solve_ms,
+                   "max_block": st.max_block, "pairs_per_matvec": st.pairs_per_matvec}
+
+    names = ("omega_x", "omega_y", "omega_z")
+    p = W.vortex_ring_3d(m=m3)
+    out = {"workload": p.name, "n_points": p.n, "nsigma_box": p.nsigma_box, "sigma_buffer": p.sigma_buffer,
+           "sigma_trunc": p.sigma_trunc, "pc": "asm (basic additive Schwarz)", "rhs": 3}
+    gm, out["mixed"] = solve(p, "mixed")
+    gd, out["fp64"] = solve(p, "fp64")
+    comp = {}
+    for k, name in enumerate(names):
+        dn = float(np.linalg.norm(gd[:, k]))
+        diff = float(np.linalg.norm(gm[:, k] - gd[:, k]))
+        comp[name] = {"weights_rel_diff_vs_fp64_gpu": diff / dn if dn > 0 else None, "weights_abs_diff": diff,
+                      "fp64_weights_norm": dn}
+    out["components_vs_fp64_gpu"] = comp
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed"]["time_s"]
+    # against the FP64 oracle at a size the host solves in the run
+    q = W.vortex_ring_3d(m=m_oracle)
+    gqm, rm = solve(q, "mixed")
+    gqd, rd = solve(q, "fp64")
+    t0 = time.perf_counter()
+    g = O.grid_for(q.x, q.y, q.z, *q.params())
+    perm, cs = O.cell_sort(g, q.x, q.y, q.z)
+    R = O.Rasm(g, q.x[perm], q.y[perm], q.z[perm], cs, basic=True)
+    orc = {"workload": q.name, "n_points": q.n, "gpu_mixed": rm, "gpu_fp64": rd}
+    for k, name in enumerate(names):
+        sol, its, reason, _ = O.gmres(g, q.x[perm], q.y[perm], q.z[perm], cs, R, q.f[perm, k], rtol=1e-12,
+                                      max_it=1000)
+        go = np.empty_like(sol)
+        go[perm] = sol
+        dn = float(np.linalg.norm(go))
+        e = {"oracle_its": its, "oracle_reason": reason}
+        for lab, gg in (("mixed", gqm), ("fp64", gqd)):
+            diff = float(np.linalg.norm(gg[:, k] - go))
+            # omega_z of a ring about the z axis is identically zero: absolute error
+            e["weights_%s_vs_oracle" % lab] = diff / dn if dn > 0 else diff
+        e["measure"] = "relative 2-norm" if dn > 0 else "absolute 2-norm (zero field)"
+        orc[name] = e
+    R.close()
+    orc["oracle_time_s"] = time.perf_counter() - t0
+    orc["oracle_cores"] = O.num_threads()
+    out["components_vs_fp64_oracle"] = orc
     return out
 
 
 def run_vortex3d(args, rank):
-    """The 3D mixed-precision form: 128^3 jittered lattice, three vortex-ring right-hand
-    sides, FP32 matvec + FP32 block Cholesky inside FP64 refinement to 1e-12, against the
-    plain FP64 GPU solve of the same problem (the form the tests pin to the oracle)."""
-    from petrbf_gb300 import workloads as W
-    from petrbf_gb300.api import Context
-    p = W.vortex_ring_3d(m=args.m3)
-    nb, sb, st_ = p.nsigma_box, p.sigma_buffer, p.sigma_trunc
-    out = {}
-    sols = {}
-    for prec in ("mixed", "fp64"):
-        with Context(dim=3, sigma=p.sigma, nsigma_box=nb, sigma_buffer=sb, sigma_trunc=st_, precision=prec,
-                     rtol=1e-12, pc="asm") as c:
-            t0 = time.perf_counter()
-            g, st = c.interpolate(p.x, p.y, p.z, p.f)
-            wall = time.perf_counter() - t0
-        sols[prec] = g
-        dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3
-        out[prec] = {"time_s": dev_s, "wall_s_incl_copies": wall, "pts_per_s": p.n / dev_s, "its": st.its,
-                     "outer_its": st.outer_its, "reason": st.reason, "true_rel_resid": st.true_rel_resid,
-                     "t_sort_ms": st.t_sort_ms, "t_setup_ms": st.t_setup_ms, "t_solve_ms": st.t_solve_ms,
-                     "max_block": st.max_block, "pairs_per_matvec": st.pairs_per_matvec}
-    gm, gd = sols["mixed"], sols["fp64"]
-    comp = {}
-    for k, name in enumerate(("omega_x", "omega_y", "omega_z")):
-        dn = float(np.linalg.norm(gd[:, k]))
-        diff = float(np.linalg.norm(gm[:, k] - gd[:, k]))
-        comp[name] = {"weights_rel_diff_vs_fp64": diff / dn if dn > 0 else None,
-                      "weights_abs_diff_vs_fp64": diff, "fp64_weights_norm": dn}
-    out["components"] = comp
-    out["mixed_speedup_vs_fp64"] = out["fp64"]["time_s"] / out["mixed"]["time_s"]
+    out = vortex3d_section(args.m3)
     print(json.dumps({"metric": "pts/s to 1e-12, 3D mixed, 3 right-hand sides", "value": out["mixed"]["pts_per_s"],
                       "unit": "pts/s", "higher_is_better": True, "dtype": "f32/f64", "data": "synthetic",
-                      "config": {"workload": p.name, "n_points": p.n, "nsigma_box": nb, "sigma_buffer": sb,
-                                 "sigma_trunc": st_, "pc": "asm (basic additive Schwarz)", "rhs": 3},
-                      "solve": out}), flush=True)
+                      "config": {"workload": out["workload"], "n_points": out["n_points"]}, "solve": out}),
+          flush=True)
 
 
-def run_batch2d(args, rank):
-    """The batched form: 256 problems of uneven N solved together (FP64, basic Schwarz), on
-    uniform-random (scattered) points and on jittered lattices of the same sizes."""
+def batch2d_section(nprob=256, max_it=1000):
+    """Config 4, the batched form: nprob problems of uneven N solved together (basic Schwarz,
+    FP64 outer residual to 1e-13), on uniform-random (scattered) points and on jittered
+    lattices of the same sizes, FP64 and mixed. The second call of each is reported (the
+    autotuner's schedule then comes from its cache; the first call's tuning time is given);
+    the batched sums' rates against the FP64 peak measured in the run."""
     import torch
     from petrbf_gb300 import workloads as W
     from petrbf_gb300.api import batch_interpolate
     peak = fp64_peak_tflops(torch)
     out = {}
-    for kind, probs in (("scattered", W.batch_scattered(nprob=args.nprob)), ("lattice", W.batch_lattice(nprob=args.nprob))):
+    for kind, probs in (("scattered", W.batch_scattered(nprob=nprob)), ("lattice", W.batch_lattice(nprob=nprob))):
         for prec in ("fp64", "mixed"):
             res = {}
-            for rep in range(2):  # second call: schedule from the autotuner's cache
+            for rep in range(2):
                 t0 = time.perf_counter()
-                g, its, reason, st = batch_interpolate(probs, rtol=1e-13, pc="asm", max_it=args.batch_max_it,
-                                                       precision=prec)
+                g, its, reason, st = batch_interpolate(probs, rtol=1e-13, pc="asm", max_it=max_it, precision=prec)
                 wall = time.perf_counter() - t0
                 res[rep] = (st, wall, its, reason)
             st, wall, its, reason = res[1]
             dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_tune_ms + st.t_solve_ms) * 1e-3
             gp = st.pairs_per_matvec / (st.t_matvec_ms * 1e-3) / 1e9
-            row = dict(st.as_dict(), pts_per_s=st.points / dev_s, wall_s=wall,
+            row = dict(st.as_dict(), pts_per_s=st.points / dev_s, time_s=dev_s, wall_s=wall,
                        first_call_tune_ms=res[0][0].t_tune_ms, its_median=float(np.median(its)),
                        its_max=int(np.max(its)), unconverged=int(np.sum(reason <= 0)),
                        matvec_gpairs_per_s=gp,
@@ -530,12 +636,52 @@ def run_batch2d(args, rank):
             if st.t_matvec32_ms > 0:
                 row["matvec32_gpairs_per_s"] = st.pairs_per_matvec / (st.t_matvec32_ms * 1e-3) / 1e9
             out["%s_%s" % (kind, prec)] = row
+    out["n_problems"] = nprob
+    return out
+
+
+def run_batch2d(args, rank):
+    out = batch2d_section(args.nprob, args.batch_max_it)
     best = max(out["scattered_fp64"]["pts_per_s"], out["scattered_mixed"]["pts_per_s"])
     print(json.dumps({"metric": "pts/s to 1e-13, batched 2D", "value": best,
                       "unit": "pts/s", "higher_is_better": True, "dtype": "f64 outer residual", "data": "synthetic",
                       "config": {"workload": "batched_2d_%d_problems" % args.nprob,
                                  "n_points": out["scattered_fp64"]["points"], "pc": "asm (basic additive Schwarz)"},
                       "batch": out}), flush=True)
+
+
+def learned_heldout_section(dev, seeds=(2001, 2002, 2003), m=2000):
+    """Config 5 on held-out problems: Lamb-Oseen fields of the training distribution (G in
+    [0.5, 2], core radius in [0.1, 0.3], centre in [-0.5, 0.5]^2) drawn with seeds outside
+    the training set (1000-1007), on 4x10^6-point jittered lattices; GMRES iterations and
+    time to 1e-13 with the learned initial guess against the zero guess, mixed and plain
+    FP64, with the off-grid error of each."""
+    from petrbf_gb300 import learned as L
+    from petrbf_gb300.api import Context
+    if not os.path.exists(L.MODEL_PATH):
+        return {"status": "no trained model"}
+    rows = []
+    for sd in seeds:
+        p = L.training_problem(sd, m=m)
+        row = {"seed": sd, "n_points": p.n, "G": p.meta["G"], "core_radius": p.meta["rc"]}
+        for prec in ("mixed", "fp64"):
+            for guess in ("zero", "learned"):
+                with Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24, precision=prec,
+                             guess=guess, device=dev) as c:
+                    if guess == "learned":
+                        L.install(c)
+                    g, st = c.interpolate(p.x, p.y, None, p.f)
+                dev_s = (st.t_sort_ms + st.t_setup_ms + st.t_solve_ms) * 1e-3  # t_solve includes the guess
+                row["%s_%s" % (prec, guess)] = {"time_s": dev_s, "its": st.its, "outer_its": st.outer_its,
+                                                "reason": st.reason, "true_rel_resid": st.true_rel_resid,
+                                                "guess_used": st.guess_used, "guess_rel_resid": st.guess_rel_resid}
+            z, l = row[prec + "_zero"], row[prec + "_learned"]
+            row[prec + "_speedup_learned_vs_zero"] = z["time_s"] / l["time_s"]
+        row["learned_mixed_vs_zero_fp64"] = row["fp64_zero"]["time_s"] / row["mixed_learned"]["time_s"]
+        rows.append(row)
+    return {"problems": rows, "seeds": list(seeds),
+            "mean_speedup_learned_vs_zero": {prec: float(np.mean([r[prec + "_speedup_learned_vs_zero"] for r in rows]))
+                                             for prec in ("mixed", "fp64")}}
 
 
 def run_seam_case(steps=10):
@@ -622,6 +768,9 @@ def run_case(name):
 
 def main():
     args = parse()
+    if args.cpu_solve_child:
+        cpu_solve_child(args)
+        return
     if args.case:
         run_case(args.case)
         return

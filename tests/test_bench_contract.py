@@ -42,3 +42,17 @@ def test_hbm_view_of_the_matvec():
     assert v["bound"] == "hbm" and v["unit"] == "GB/s" and v["bytes_per_launch"] == 128_000_000
     assert abs(v["achieved"] - 128e6 / 44.8e-3 / 1e9) < 1e-9
     assert v["peak"] > 0 and abs(v["frac"] - v["achieved"] / v["peak"]) < 1e-12
+
+
+def test_host_core_solve_child_small(tmp_path):
+    """The child process that solves the 4x10^6-point problem on the host cores (memory
+    guard, address-space cap, weights file), here on a 3600-point lattice."""
+    out = str(tmp_path / "cpu.json")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-solve-child", out, "--m", "60",
+                        "--seed", "5"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.load(open(out))
+    assert d["status"] == "ok" and d["reason"] == 2 and d["its"] > 0 and d["setup_status"] == 0
+    import numpy as np
+    g = np.load(out + ".g.npy")
+    assert g.shape == (3600,) and np.all(np.isfinite(g))
