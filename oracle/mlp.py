@@ -6,6 +6,11 @@ W[out][in] row-major then b[out]; the forward pass uses the weights rounded to B
 (round to nearest even), the biases in FP32; the loss is the masked mean-squared error.
 Gradients are taken with respect to the FP32 master weights through the BF16 rounding
 (straight-through), as the CUDA backward does.
+
+bf16_operands (the CUDA network's tensor-core GEMMs): every GEMM operand is rounded to BF16
+as the network rounds it -- the features and hidden activations entering a layer, and the
+output gradient dZ entering dW = dZ^T H and dH = dZ W -- while the products are summed in
+FP64 here (FP32 on the GPU), the ReLU masks, biases and bias gradients stay unrounded.
 """
 import numpy as np
 
@@ -30,30 +35,36 @@ def unpack(w, round_weights=True):
     return out
 
 
-def forward(w, X, round_weights=True):
+def _op(a, on):
+    """A GEMM operand: rounded to BF16 (through FP32) when the GPU rounds it."""
+    return bf16(np.asarray(a, np.float32)) if on else np.asarray(a, np.float64)
+
+
+def forward(w, X, round_weights=True, bf16_operands=True):
     acts, h = [], np.asarray(X, np.float64)
     layers = unpack(w, round_weights)
     for k, (W, b) in enumerate(layers):
-        z = h @ W.T + b
+        z = _op(h, bf16_operands) @ W.T + b
         h = np.maximum(z, 0.0) if k < len(layers) - 1 else z
         acts.append(h)
     return acts
 
 
-def loss_grad(w, X, T, M, round_weights=True):
+def loss_grad(w, X, T, M, round_weights=True, bf16_operands=True):
     X, T, M = (np.asarray(a, np.float64) for a in (X, T, M))
     layers = unpack(w, round_weights)
-    acts = forward(w, X, round_weights)
+    acts = forward(w, X, round_weights, bf16_operands)
     cnt = M.sum()
     d = (acts[-1] - T) * M
     loss = (d * d).sum() / cnt
     dz = 2.0 * d / cnt
     grads = [None] * len(layers)
     for k in range(len(layers) - 1, -1, -1):
-        hin = acts[k - 1] if k > 0 else X
+        hin = _op(acts[k - 1] if k > 0 else X, bf16_operands)
         W, _ = layers[k]
-        grads[k] = (dz.T @ hin, dz.sum(axis=0))
+        dzo = _op(dz, bf16_operands)
+        grads[k] = (dzo.T @ hin, dz.sum(axis=0))
         if k > 0:
-            dz = (dz @ W) * (acts[k - 1] > 0)
+            dz = (dzo @ W) * (acts[k - 1] > 0)
     flat = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
     return loss, flat

@@ -31,6 +31,7 @@
 
 #include "krylov.h"
 #include "rasm.h"
+#include "trace.h"
 
 namespace prbf {
 
@@ -205,6 +206,7 @@ Schedule autotune(Ctx& c, BatchState& B, const double* vin, double* vout, bool f
 void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_out, int* reason_out,
                        prbf_batch_stats* bs) {
   const double t_begin = now_ms();
+  TraceRange tr_cluster("batch InitCluster");
   const prbf_params& p = c.p;
   const int dim = p.dim;
   if (nprob <= 0 || !probs) throw Error(PRBF_ERR_ARG, "empty batch");
@@ -330,6 +332,8 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   loc.clear();
   const double t_sorted = now_ms();
+  tr_cluster.end();
+  TraceRange tr_mat("batch InitMat");
   BlockGeom G;
   G.dim = dim;
   G.n = N;
@@ -347,6 +351,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   rasm_set_apply_smem(B.rasm);
   c.check_device_error("batch RASM set-up");
   const double t_setup = now_ms();
+  tr_mat.end();
 
   // ---- operator, schedule, Krylov segments ---------------------------------------------
   B.op.plan = &B.plan;
@@ -381,6 +386,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   }
   if (!cached) {
     const double tt0 = now_ms();
+    TraceRange tr_tune("batch autotune");
     sch = autotune(c, B, B.b.get(), B.tmp.get(), mixed);
     t_tune = now_ms() - tt0;
     std::lock_guard<std::mutex> lk(schedule_mutex());
@@ -421,6 +427,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   B.rasm.seg = seg;
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double ts0 = now_ms();
+  TraceRange tr_solve("batch KSPSolve");
   std::vector<int> its(nprob, 0), reason(nprob, 0), outer(nprob, 0);
   std::vector<char> to64(nprob, 0);  // mixed form: problems handed to the FP64 batch
   std::vector<double> true_rel(nprob, 0.0);
@@ -525,6 +532,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   }
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double t_solve = now_ms() - ts0;
+  tr_solve.end();
   B.plan.seg = SegSkip{};
   B.rasm.seg = SegSkip{};
   B.kry.reset_graph();  // the captured launches carry the stop flags

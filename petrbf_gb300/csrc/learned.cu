@@ -50,7 +50,7 @@ void guess_compute(Ctx& c, Mlp& net, int n, const double* x, const double* y, co
   net.forward(X.get(), nc, c.stream);
   unpatch_dev(c, P, cells.get(), nc, net.out(), sc.get(), gf.get());
   scatter_dev(n, P.perm.get(), gf.get(), g, c.stream);
-  PRBF_CUDA(cudaStreamSynchronize(c.stream));
+  net.check(c.stream);
 }
 
 }  // namespace prbf
@@ -155,7 +155,7 @@ int prbf_mlp_forward(prbf_mlp* m, int n, const float* X, float* Y) {
     upload_f(q.X, X, (size_t)n * MLP_IN, q.stream);
     q.net.forward(q.X.get(), n, q.stream);
     PRBF_CUDA(cudaMemcpyAsync(Y, q.net.out(), sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost, q.stream));
-    PRBF_CUDA(cudaStreamSynchronize(q.stream));
+    q.net.check(q.stream);
   });
 }
 
@@ -176,7 +176,7 @@ int prbf_mlp_loss_grad(prbf_mlp* m, int n, const float* X, const float* T, const
     if (grad_out)
       PRBF_CUDA(cudaMemcpyAsync(grad_out, q.net.grad.get(), sizeof(float) * mlp_param_count(), cudaMemcpyDeviceToHost,
                                 q.stream));
-    PRBF_CUDA(cudaStreamSynchronize(q.stream));
+    q.net.check(q.stream);
   });
 }
 
@@ -223,7 +223,7 @@ int prbf_mlp_train(prbf_mlp* m, int n, const float* X, const float* T, const flo
       }
       float l = 0;
       PRBF_CUDA(cudaMemcpyAsync(&l, q.loss.get(), sizeof(float), cudaMemcpyDeviceToHost, s));
-      PRBF_CUDA(cudaStreamSynchronize(s));
+      q.net.check(s);
       if (loss_per_epoch) loss_per_epoch[ep] = nbatch ? l / nbatch : 0.f;
     }
   });

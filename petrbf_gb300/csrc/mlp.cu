@@ -11,11 +11,15 @@
 // would make t unbounded where the local field is small but the weights still carry the
 // tail of A^-1 applied to the field nearby.)
 // Network: 256 -> 256 -> 256 -> 256 -> 16, ReLU after the three hidden layers; BF16
-// weights (an FP32 master copy for Adam), FP32 activations and accumulation. All GEMMs are
-// one tiled kernel (64 x 64 output tile per CTA, 4 x 4 outputs per thread, operands staged
-// through shared memory with register prefetch).
+// weights (an FP32 master copy for Adam). Every GEMM of the forward and backward passes runs
+// on the tensor cores (gemm_bf16_tc, tcgen05.mma kind::f16: BF16 operands, FP32
+// accumulation): the features, activations and output gradients are rounded to BF16 as
+// GEMM operands; the activations, biases, loss, bias gradients and weight gradients stay
+// FP32. The weight gradient dW = dZ^T H and the input gradient dH = dZ W take K-major
+// operands, so dZ, H and W are also kept transposed (BF16).
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -24,106 +28,6 @@
 
 namespace prbf {
 namespace {
-
-constexpr int GT = 64;    // output tile
-constexpr int GK = 16;    // inner chunk
-constexpr int GTH = 256;  // threads (16 x 16, 4 x 4 outputs each)
-
-__device__ __forceinline__ float to_f(float v) { return v; }
-__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
-
-// C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]) (ReLU if relu); beta: C = beta C + ...
-// A(m, k) = tA ? A[k lda + m] : A[m lda + k];  B(k, n) = tB ? B[n ldb + k] : B[k ldb + n]
-template <class TB_, bool tA, bool tB>
-__global__ void __launch_bounds__(GTH) k_gemm(int M, int N, int K, const float* __restrict__ A, int lda,
-                                              const TB_* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
-                                              const float* __restrict__ bias, int relu, float beta) {
-  __shared__ float As[2][GK][GT + 4];
-  __shared__ float Bs[2][GK][GT + 4];
-  const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
-  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-  float acc[4][4] = {};
-  float ra[4], rb[4];
-  auto fetch = [&](int k0) {
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      int e = threadIdx.x + q * GTH;  // 1024 = GK x GT
-      int r, k;
-      if (!tA) {
-        k = e % GK;
-        r = e / GK;
-      } else {
-        r = e % GT;
-        k = e / GT;
-      }
-      int gm = m0 + r, gk = k0 + k;
-      ra[q] = (gm < M && gk < K) ? (tA ? A[(long long)gk * lda + gm] : A[(long long)gm * lda + gk]) : 0.f;
-      int c, kb;
-      if (tB) {
-        kb = e % GK;
-        c = e / GK;
-      } else {
-        c = e % GT;
-        kb = e / GT;
-      }
-      int gn = n0 + c, gkb = k0 + kb;
-      rb[q] = (gn < N && gkb < K) ? to_f(tB ? B[(long long)gn * ldb + gkb] : B[(long long)gkb * ldb + gn]) : 0.f;
-    }
-  };
-  auto store = [&](int buf) {
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      int e = threadIdx.x + q * GTH;
-      int r = tA ? e % GT : e / GK, k = tA ? e / GT : e % GK;
-      As[buf][k][r] = ra[q];
-      int c = tB ? e / GK : e % GT, kb = tB ? e % GK : e / GT;
-      Bs[buf][kb][c] = rb[q];
-    }
-  };
-  const int nch = (K + GK - 1) / GK;
-  if (nch > 0) fetch(0);
-  for (int ch = 0; ch < nch; ch++) {
-    int buf = ch & 1;
-    store(buf);
-    __syncthreads();
-    if (ch + 1 < nch) fetch((ch + 1) * GK);
-#pragma unroll
-    for (int k = 0; k < GK; k++) {
-      float a[4], b[4];
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        a[q] = As[buf][k][ty * 4 + q];
-        b[q] = Bs[buf][k][tx * 4 + q];
-      }
-#pragma unroll
-      for (int p = 0; p < 4; p++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) acc[p][q] = fmaf(a[p], b[q], acc[p][q]);
-    }
-  }
-#pragma unroll
-  for (int p = 0; p < 4; p++) {
-    int m = m0 + ty * 4 + p;
-    if (m >= M) continue;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      int n = n0 + tx * 4 + q;
-      if (n >= N) continue;
-      float v = acc[p][q] + (bias ? bias[n] : 0.f);
-      if (relu) v = fmaxf(v, 0.f);
-      float* o = C + (long long)m * ldc + n;
-      *o = beta != 0.f ? beta * *o + v : v;
-    }
-  }
-}
-
-template <class TB_, bool tA, bool tB>
-void gemm(int M, int N, int K, const float* A, int lda, const TB_* B, int ldb, float* C, int ldc, const float* bias,
-          bool relu, float beta, cudaStream_t s) {
-  dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
-  k_gemm<TB_, tA, tB><<<grid, GTH, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, relu ? 1 : 0, beta);
-  PRBF_CHECK_LAUNCH();
-}
 
 // dY = 2 mask (Y - T) / sum(mask); loss partial sums
 __global__ void k_mse(int n, const float* __restrict__ Y, const float* __restrict__ T, const float* __restrict__ Msk,
@@ -168,8 +72,38 @@ __global__ void k_adam(int n, float* __restrict__ w, const float* __restrict__ g
   }
 }
 
-__global__ void k_to_bf16(int n, const float* __restrict__ w, __nv_bfloat16* __restrict__ wb) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) wb[i] = __float2bfloat16_rn(w[i]);
+__global__ void k_to_bf16(long long n, const float* __restrict__ w, __nv_bfloat16* __restrict__ wb) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// dst[c][r] = src[r][c] for a rows x cols BF16 matrix (leading dimensions lds, ldd); 32 x 32
+// tiles through shared memory, 32 x 8 threads.
+__global__ void k_transpose_bf16(int rows, int cols, const __nv_bfloat16* __restrict__ src, int lds,
+                                 __nv_bfloat16* __restrict__ dst, int ldd) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[k][threadIdx.x] = src[(long long)r * lds + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(long long)c * ldd + r] = t[threadIdx.x][k];
+  }
+}
+
+void transpose_bf16(int rows, int cols, const __nv_bfloat16* src, int lds, __nv_bfloat16* dst, int ldd,
+                    cudaStream_t s) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose_bf16<<<grid, dim3(32, 8), 0, s>>>(rows, cols, src, lds, dst, ldd);
+  PRBF_CHECK_LAUNCH();
+}
+
+void to_bf16(long long n, const float* src, __nv_bfloat16* dst, cudaStream_t s) {
+  k_to_bf16<<<(int)std::min<long long>((n + 255) / 256, 4 * 152), 256, 0, s>>>(n, src, dst);
+  PRBF_CHECK_LAUNCH();
 }
 
 // ---- patches ----------------------------------------------------------------------------
@@ -309,11 +243,32 @@ void Mlp::init(uint64_t seed, cudaStream_t s) {
 void Mlp::set_weights(const float* host, cudaStream_t s) {
   size_t np = mlp_param_count();
   w.reserve(np);
-  wb.reserve(np);
   PRBF_CUDA(cudaMemcpyAsync(w.get(), host, sizeof(float) * np, cudaMemcpyHostToDevice, s));
-  k_to_bf16<<<256, 256, 0, s>>>((int)np, w.get(), wb.get());
-  PRBF_CHECK_LAUNCH();
+  refresh_bf16(s);
+  if (!err.get()) {
+    err.reserve(4);
+    PRBF_CUDA(cudaMemsetAsync(err.get(), 0, 16, s));
+  }
   ready = true;
+}
+
+void Mlp::refresh_bf16(cudaStream_t s) {
+  const size_t np = mlp_param_count();
+  wb.reserve(np);
+  wbT.reserve(np);
+  to_bf16((long long)np, w.get(), wb.get(), s);
+  for (int l = 0; l < MLP_LAYERS; l++)
+    transpose_bf16(kLayerOut[l], kLayerIn[l], wb.get() + woff(l), kLayerIn[l], wbT.get() + woff(l), kLayerOut[l], s);
+}
+
+void Mlp::check(cudaStream_t s) {
+  unsigned h = 0;
+  PRBF_CUDA(cudaMemcpyAsync(&h, err.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  if (h) {
+    PRBF_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(unsigned), s));
+    throw Error(PRBF_ERR_TIMEOUT, "network GEMM: bounded device wait gave up");
+  }
 }
 
 size_t Mlp::woff(int l) const {
@@ -322,17 +277,21 @@ size_t Mlp::woff(int l) const {
   return o;
 }
 
-// Forward for n rows of X (device); H[l] activations are kept for the backward pass.
+// Forward for n rows of X (device); the activations (FP32, and BF16 as the next GEMM's
+// operand) are kept for the backward pass.
 void Mlp::forward(const float* X, int n, cudaStream_t s) {
-  for (int l = 0; l < MLP_LAYERS; l++) acts[l].reserve((size_t)n * kLayerOut[l]);
-  const float* in = X;
+  xb.reserve((size_t)n * MLP_IN);
+  to_bf16((long long)n * MLP_IN, X, xb.get(), s);
+  const __nv_bfloat16* in = xb.get();
   for (int l = 0; l < MLP_LAYERS; l++) {
-    size_t o = woff(l);
-    const __nv_bfloat16* W = wb.get() + o;
+    acts[l].reserve((size_t)n * kLayerOut[l]);
+    const bool hidden = l < MLP_LAYERS - 1;
+    if (hidden) actb[l].reserve((size_t)n * kLayerOut[l]);
+    const size_t o = woff(l);
     const float* b = w.get() + o + (size_t)kLayerIn[l] * kLayerOut[l];
-    gemm<__nv_bfloat16, false, true>(n, kLayerOut[l], kLayerIn[l], in, kLayerIn[l], W, kLayerIn[l], acts[l].get(),
-                                     kLayerOut[l], b, l < MLP_LAYERS - 1, 0.f, s);
-    in = acts[l].get();
+    gemm_bf16_tc(n, kLayerOut[l], kLayerIn[l], in, kLayerIn[l], wb.get() + o, kLayerIn[l], acts[l].get(),
+                 kLayerOut[l], hidden ? actb[l].get() : nullptr, kLayerOut[l], b, hidden, err.get(), s);
+    if (hidden) in = actb[l].get();
   }
 }
 
@@ -346,19 +305,27 @@ void Mlp::backward(const float* X, const float* T, const float* Msk, int n, floa
   k_mse<<<256, 256, 0, s>>>(n * MLP_OUT, acts[MLP_LAYERS - 1].get(), T, Msk, inv_cnt, dY, dloss);
   PRBF_CHECK_LAUNCH();
   (void)np;
+  (void)X;  // its BF16 copy from the forward pass is the first layer's operand
+  const int ldn = (n + 7) / 8 * 8;  // transposed operands: rows padded to 16 bytes
+  dzb.reserve((size_t)n * MLP_HID);
+  dzT.reserve((size_t)MLP_HID * ldn);
+  hT.reserve((size_t)MLP_HID * ldn);
   float* dcur = dY;
   for (int l = MLP_LAYERS - 1; l >= 0; l--) {
     const int K = kLayerIn[l], N = kLayerOut[l];
-    const float* Hin = l > 0 ? acts[l - 1].get() : X;
+    const __nv_bfloat16* Hin = l > 0 ? actb[l - 1].get() : xb.get();
     size_t o = woff(l);
-    // dW[N][K] = dZ^T Hin ; db = colsum dZ
-    gemm<float, true, false>(N, K, n, dcur, N, Hin, K, grad.get() + o, K, nullptr, false, 0.f, s);
+    to_bf16((long long)n * N, dcur, dzb.get(), s);
+    transpose_bf16(n, N, dzb.get(), N, dzT.get(), ldn, s);
+    transpose_bf16(n, K, Hin, K, hT.get(), ldn, s);
+    // dW[N][K] = dZ^T Hin (the batch is the inner dimension) ; db = colsum dZ (FP32)
+    gemm_bf16_tc(N, K, n, dzT.get(), ldn, hT.get(), ldn, grad.get() + o, K, nullptr, 0, nullptr, false, err.get(), s);
     k_colsum<<<(N + 127) / 128, 128, 0, s>>>(n, N, dcur, grad.get() + o + (size_t)K * N);
     PRBF_CHECK_LAUNCH();
     if (l > 0) {
       float* dprev = dact[(MLP_LAYERS - l) & 1].get();
-      // dH = dZ W  (W is [N][K] BF16)
-      gemm<__nv_bfloat16, false, false>(n, K, N, dcur, N, wb.get() + o, K, dprev, K, nullptr, false, 0.f, s);
+      // dH[n][K] = dZ W, W^T [K][N] as the K-major operand
+      gemm_bf16_tc(n, K, N, dzb.get(), N, wbT.get() + o, N, dprev, K, nullptr, 0, nullptr, false, err.get(), s);
       k_relu_back<<<256, 256, 0, s>>>(n * K, acts[l - 1].get(), dprev);
       PRBF_CHECK_LAUNCH();
       dcur = dprev;
@@ -370,9 +337,10 @@ void Mlp::adam(float lr, cudaStream_t s) {
   step++;
   const float b1 = 0.9f, b2 = 0.999f;
   float c1 = 1.f / (1.f - std::pow(b1, (float)step)), c2 = 1.f / (1.f - std::pow(b2, (float)step));
-  k_adam<<<256, 256, 0, s>>>((int)mlp_param_count(), w.get(), grad.get(), m1.get(), m2.get(), wb.get(), lr, b1, b2, c1,
+  k_adam<<<256, 256, 0, s>>>((int)mlp_param_count(), w.get(), grad.get(), m1.get(), m2.get(), nullptr, lr, b1, b2, c1,
                              c2, 1e-8f);
   PRBF_CHECK_LAUNCH();
+  refresh_bf16(s);
 }
 
 int fine_cells(Ctx& c, PointSet& P, Workspace& ws, DevBuf<int>& cells) {

@@ -18,13 +18,16 @@ extern const int kLayerOut[MLP_LAYERS];
 size_t mlp_param_count();
 
 // Network state: FP32 master weights (per layer: W[out][in] row-major, then b[out]), their
-// BF16 copy used by the GEMMs, Adam moments, gradients and the activations of the last
-// forward pass.
+// BF16 copy W and its transpose W^T (same offsets, [in][out]) used by the tensor-core
+// GEMMs, Adam moments, gradients, the FP32 activations of the last forward pass and their
+// BF16 copies (the GEMM operands), and the device error word of the GEMMs.
 struct Mlp {
   DevBuf<float> w, grad, m1, m2;
-  DevBuf<__nv_bfloat16> wb;
+  DevBuf<__nv_bfloat16> wb, wbT;
   DevBuf<float> acts[MLP_LAYERS];
   DevBuf<float> dact[2];
+  DevBuf<__nv_bfloat16> xb, actb[MLP_LAYERS - 1], dzb, dzT, hT;
+  DevBuf<unsigned> err;
   int step = 0;
   bool ready = false;
   void init(uint64_t seed, cudaStream_t s);
@@ -33,8 +36,20 @@ struct Mlp {
   void forward(const float* X, int n, cudaStream_t s);
   void backward(const float* X, const float* T, const float* Msk, int n, float inv_cnt, float* dloss, cudaStream_t s);
   void adam(float lr, cudaStream_t s);
+  // raises PRBF_ERR_TIMEOUT if a GEMM's bounded wait gave up since the last check (syncs s)
+  void check(cudaStream_t s);
   const float* out() const { return acts[MLP_LAYERS - 1].get(); }
+
+ private:
+  void refresh_bf16(cudaStream_t s);  // wb and wbT from w
 };
+
+// C[M][N] = A[M][K] B[N][K]^T (+ bias, ReLU) on the tensor cores (gemm_tc.cu): A and B
+// BF16 row-major with K contiguous (leading dimensions lda, ldb multiples of 8, 16-byte
+// aligned bases), FP32 accumulation; C (FP32, ldc) and/or Cb (BF16, ldcb) may be null.
+// N <= 256; entries past the matrix edges read as zero.
+void gemm_bf16_tc(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C,
+                  int ldc, __nv_bfloat16* Cb, int ldcb, const float* bias, bool relu, unsigned* err, cudaStream_t s);
 
 // Non-empty fine cells of P (compacted list), returns their count.
 int fine_cells(Ctx& c, PointSet& P, Workspace& ws, DevBuf<int>& cells);

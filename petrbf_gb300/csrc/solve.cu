@@ -22,6 +22,7 @@
 #include "krylov.h"
 #include "mlp.h"
 #include "rasm.h"
+#include "trace.h"
 
 namespace prbf {
 
@@ -83,6 +84,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   SolveState& S = *c.solve;
   // ---- cell list -----------------------------------------------------------------------
   {
+    TraceRange tr("InitCluster");
     DevBuf<double> ux, uy, uz;
     c.upload(ux, x, n);
     c.upload(uy, y, n);
@@ -95,6 +97,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   }
   const double t_sorted = now_ms();
   // ---- operator and RASM set-up ----------------------------------------------------------
+  TraceRange tr_mat("InitMat");
   S.plan.g = S.pts.g;
   S.plan.sym_nv = std::min(4, nrhs);  // right-hand sides summed together by the symmetric form
   gauss_plan_dev(S.plan, S.pts.view(), S.pts.view(), c.err.get(), c.ws, c.stream);
@@ -110,6 +113,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   rasm_set_apply_smem(S.rasm);
   c.check_device_error("RASM set-up");
   const double t_setup = now_ms();
+  tr_mat.end();
 
   // right-hand sides: segments of one vector at a 32-aligned stride, solved in lockstep
   // (the matvec computes each pair's exponential once for all of them)
@@ -154,6 +158,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   PRBF_CUDA(cudaMemsetAsync(S.tmp.get(), 0, sizeof(double) * len_all, c.stream));
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double ts0 = now_ms();
+  TraceRange tr_solve("KSPSolve");
   if (use_guess) {
     // x0 from the network, in the solver's cell order (its inputs are the sorted points)
     for (int v = 0; v < nv; v++)
@@ -300,6 +305,8 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   }
   PRBF_CUDA(cudaStreamSynchronize(c.stream));
   const double t_solve = now_ms() - ts0;
+  tr_solve.end();
+  TraceRange tr_post("Post Processing");
   c.check_device_error("solve");
   // weights back in the caller's order (2d/rbf_interpolation.cxx:246-265)
   for (int v = 0; v < nv; v++) {

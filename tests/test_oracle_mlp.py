@@ -11,12 +11,12 @@ def test_oracle_gradient_matches_finite_differences():
     X = rng.standard_normal((6, 256))
     T = rng.standard_normal((6, 16))
     M = (rng.uniform(size=(6, 16)) < 0.7).astype(float)
-    loss, g = OM.loss_grad(w, X, T, M, round_weights=False)
+    loss, g = OM.loss_grad(w, X, T, M, round_weights=False, bf16_operands=False)
     for idx in rng.choice(n_par, 12, replace=False):
         e = np.zeros(n_par)
         e[idx] = 1e-6
-        lp, _ = OM.loss_grad(w + e, X, T, M, round_weights=False)
-        lm, _ = OM.loss_grad(w - e, X, T, M, round_weights=False)
+        lp, _ = OM.loss_grad(w + e, X, T, M, round_weights=False, bf16_operands=False)
+        lm, _ = OM.loss_grad(w - e, X, T, M, round_weights=False, bf16_operands=False)
         fd = (lp - lm) / 2e-6
         assert abs(fd - g[idx]) <= 1e-6 + 1e-5 * abs(fd), (idx, fd, g[idx])
 
