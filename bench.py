@@ -758,6 +758,13 @@ def run_case(name):
         batch_interpolate(W.batch_scattered(nprob=24, nmax=60000), rtol=1e-13, pc="asm")
     elif name == "batch_mixed":  # 24 jittered-lattice problems of the batched form, mixed
         batch_interpolate(W.batch_lattice(nprob=24, nmax=60000), rtol=1e-13, pc="asm", precision="mixed")
+    elif name == "mlp_guess":  # learned-guess inference on a 10^6-point lattice (tensor-core GEMMs)
+        from petrbf_gb300 import learned as L
+        p = L.training_problem(2001, m=1000)
+        with Context(dim=2, sigma=p.sigma, guess="learned") as c:
+            L.install(c)
+            for _ in range(3):
+                L.guess(c, p.x, p.y, p.f)
     elif name == "seam_2d":  # the gpumatmult seam on the packed arrays of a 10^6-point lattice
         run_seam_case()
         return

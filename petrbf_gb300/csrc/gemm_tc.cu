@@ -25,7 +25,7 @@ namespace {
 
 constexpr int GM = 128;     // rows per CTA (TMEM lanes)
 constexpr int GKC = 64;     // K per stage: 64 BF16 = 128 bytes, one swizzle row
-constexpr int GSTAGES = 3;  // ring depth
+constexpr int GSTAGES = 2;  // ring depth (two CTAs share an SM at N = 256)
 constexpr int GTHREADS = 128;
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -175,7 +175,11 @@ __global__ void __launch_bounds__(GTHREADS, 1)
   const bool ok = mbar_wait(&done, 0);
   if (!ok && lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + 32 * w + lane;
+  // Each 16-column slice of the warp's 32 rows goes through shared memory (the ring is idle
+  // once the last MMA has completed), so that a store instruction writes two rows of 16
+  // consecutive columns instead of one column of 32 rows.
+  float* stg = (float*)(sm + w * (32 * 17 * 4));
+  const int half = lane >> 4, cl = lane & 15;
   // tcgen05.ld is warp-collective: the whole warp takes the same branch
   if (__all_sync(0xffffffffu, ok && !s_abort)) {
 #pragma unroll 1
@@ -188,17 +192,23 @@ __global__ void __launch_bounds__(GTHREADS, 1)
             "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
           : "r"(addr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int n = c0 + j;
-          if (n >= N) break;
-          float v = __uint_as_float(r[j]) + (bias ? bias[n] : 0.f);
+      for (int j = 0; j < 16; j++) stg[lane * 17 + j] = __uint_as_float(r[j]);
+      __syncwarp();
+      const int n = c0 + cl;
+      const float bn = (bias && n < N) ? bias[n] : 0.f;
+#pragma unroll 4
+      for (int rr = 0; rr < 32; rr += 2) {
+        const int rloc = rr + half;
+        const long long row = m0 + 32 * w + rloc;
+        if (row < M && n < N) {
+          float v = stg[rloc * 17 + cl] + bn;
           if (relu) v = fmaxf(v, 0.f);
-          if (C) C[(long long)row * ldc + n] = v;
-          if (Cb) Cb[(long long)row * ldcb + n] = __float2bfloat16_rn(v);
+          if (C) C[row * ldc + n] = v;
+          if (Cb) Cb[row * ldcb + n] = __float2bfloat16_rn(v);
         }
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
