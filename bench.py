@@ -31,7 +31,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = 15  # the reference's count per pair, exp counted as 1 (2d/matmult.cxx:44-45)
-CPU_SAMPLE_M = 1000  # CPU baseline sample: 1000 x 1000 jittered lattice, same geometry
 
 
 def parse():
@@ -179,16 +178,25 @@ def profile_traffic(name):
     return None
 
 
-def cpu_baseline(seconds_target=10.0):
-    """The oracle (C++ restatement of mymatmult, OpenMP over cells) on a bounded sample:
-    a 1000 x 1000 jittered lattice with the workload's geometry (same pairs per point)."""
+def workload_name(m):
+    return "2d_lamb_oseen_N4e6_jitter" if m == 2000 else "2d_lamb_oseen_m%d" % m
+
+
+def _cpu_matvec_setup(p):
+    """Cell list of the workload on the host (the oracle's cell sort) and its pair count."""
     import oracle as O
-    from petrbf_gb300 import workloads as W
-    p = W.lamb_oseen_2d(CPU_SAMPLE_M, jitter=0.25, seed=12345)
     g = O.grid_for(p.x, p.y, None, *p.params())
     perm, cs = O.cell_sort(g, p.x, p.y)
     xs, ys = p.x[perm], p.y[perm]
     pairs = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
+    return g, xs, ys, cs, pairs
+
+
+def cpu_baseline(p, seconds_target=10.0):
+    """The oracle (C++ restatement of mymatmult, OpenMP over cells) on the workload itself,
+    every point; the sample is the number of matvecs, bounded by seconds_target."""
+    import oracle as O
+    g, xs, ys, cs, pairs = _cpu_matvec_setup(p)
     v = np.random.default_rng(1).standard_normal(p.n)
     O.matvec(g, xs, ys, None, cs, v)  # warm
     t0 = time.perf_counter()
@@ -201,22 +209,20 @@ def cpu_baseline(seconds_target=10.0):
     dt = time.perf_counter() - t0
     return {"value": pairs * reps / dt / 1e9, "unit": "Gpairs/s", "cores": O.num_threads(),
             "kind": "port",
-            "sample": "%d FP64 matvecs of a %dx%d jittered lattice (%.3g pairs each), %.1f s" % (
-                reps, CPU_SAMPLE_M, CPU_SAMPLE_M, pairs, dt)}
+            "sample": "%d FP64 matvecs of the full %d-point workload (%.3g pairs each), %.1f s" % (
+                reps, p.n, pairs, dt)}
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU matvec (the oracle port; the reference's
-    compiled sources are not available on this machine) on all host cores."""
+    """--impl reference: the reference's CPU matvec (the oracle port: the reference's compiled
+    sources do not travel to an Arm host) on all host cores, over the same workload as the
+    GPU arm -- every point, every step."""
     if rank != 0:
         return
     import oracle as O
     from petrbf_gb300 import workloads as W
-    p = W.lamb_oseen_2d(CPU_SAMPLE_M, jitter=0.25, seed=12345)
-    g = O.grid_for(p.x, p.y, None, *p.params())
-    perm, cs = O.cell_sort(g, p.x, p.y)
-    xs, ys = p.x[perm], p.y[perm]
-    pairs = int((np.diff(cs) * O.trunc_counts(g, xs, ys, None, cs)).sum())
+    p = W.lamb_oseen_2d(args.m, jitter=0.25, seed=12345)
+    g, xs, ys, cs, pairs = _cpu_matvec_setup(p)
     v = np.random.default_rng(1).standard_normal(p.n)
     for _ in range(args.warmup):
         O.matvec(g, xs, ys, None, cs, v)
@@ -225,15 +231,14 @@ def run_reference(args, rank, world):
         O.matvec(g, xs, ys, None, cs, v)
     dt = time.perf_counter() - t0
     val = pairs * args.steps / dt / 1e9
-    sample = "%d FP64 matvecs of a %dx%d jittered lattice (%.3g pairs each)" % (
-        args.steps, CPU_SAMPLE_M, CPU_SAMPLE_M, pairs)
+    sample = "%d FP64 matvecs of the full %d-point workload (%.3g pairs each)" % (args.steps, p.n, pairs)
     print(json.dumps({
         "impl": "reference", "metric": "Gaussian matvec Gpairs/s", "value": val, "unit": "Gpairs/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "2d_lamb_oseen_N4e6_jitter matvec (CPU sample N=1e6, same geometry)",
-                   "sigma_over_h": 1.25, "nsigma_box": 8, "sigma_buffer": 24, "sigma_trunc": 24},
+        "config": {"workload": workload_name(args.m), "n_points": p.n, "sigma_over_h": 1.25,
+                   "nsigma_box": 8, "sigma_buffer": 24, "sigma_trunc": 24, "pairs_per_matvec": pairs},
         "cpu_baseline": {"value": val, "unit": "Gpairs/s", "cores": O.num_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": val, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -329,7 +334,7 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "2d_lamb_oseen_N4e6_jitter" if args.m == 2000 else "2d_lamb_oseen_m%d" % args.m,
+        "config": {"workload": workload_name(args.m),
                    "n_points": n, "sigma_over_h": 1.25, "nsigma_box": 8, "sigma_buffer": 24,
                    "sigma_trunc": 24, "pairs_per_matvec": pairs, "ncell": info["ncell"],
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
@@ -351,7 +356,7 @@ def run_ours(args, rank, world):
         "wall_s_timed_region": t_wall,
     }
     if rank == 0 and world == 1:
-        result["cpu_baseline"] = cpu_baseline()
+        result["cpu_baseline"] = cpu_baseline(p)
     sections = set() if args.skip_solve else set(args.sections.split(","))
     if "solve" in sections:
         result["solve"], g64 = solve_section(p, dev, rank)
