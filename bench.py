@@ -770,6 +770,12 @@ def run_case(name):
             L.install(c)
             for _ in range(3):
                 L.guess(c, p.x, p.y, p.f)
+    elif name in ("mixed3d", "mixed3d_small"):  # the 3D mixed solve: vortex ring, 3 right-hand sides, to 1e-12
+        p = W.vortex_ring_3d(m=128 if name == "mixed3d" else 48)  # 128^3 (2.1x10^6 points) or 48^3
+        with Context(dim=3, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+                     sigma_trunc=p.sigma_trunc, precision="mixed", rtol=1e-12, pc="asm") as c:
+            _, st = c.interpolate(p.x, p.y, p.z, p.f)
+        print("its", st.its, "outer", st.outer_its, "solve_ms", st.t_solve_ms, "setup_ms", st.t_setup_ms)
     elif name == "seam_2d":  # the gpumatmult seam on the packed arrays of a 10^6-point lattice
         run_seam_case()
         return

@@ -18,6 +18,7 @@
 // fixed order (deterministic, and for one segment the same blocks as a single solve).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "krylov.h"
@@ -40,21 +41,46 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;  // valid in thread 0
 }
 
-// part[b*(m+1) + j] = sum over block b's range of V_j . w, j <= k
+// part[b*(m+1) + j] = sum over block b's range of V_j . w, j <= k. The basis vectors are
+// taken JG at a time: one pass over the block's range reads w once and V_j0..V_j0+JG-1 into
+// JG accumulators, and one block reduction serves all JG of them. Each accumulator sees its
+// products in the same order as a loop over one j would, and each partial sum is the warp
+// sum followed by the warps' sums in warp order, so the result does not depend on JG.
+constexpr int JG = 16;
+
 __global__ void __launch_bounds__(KT) k_multidot(const KGlob* __restrict__ G, const KSeg* __restrict__ S,
                                                  const int* __restrict__ bseg, const int2* __restrict__ brange,
                                                  const double* __restrict__ V, long long ld, const double* __restrict__ w,
                                                  double* __restrict__ part, int mp1) {
   if (G->done || S[bseg[blockIdx.x]].done) return;
-  __shared__ double sh[KT / 32];
+  __shared__ double sh[JG][KT / 32];
   const int k = G->k;
   const int2 rg = brange[blockIdx.x];
-  for (int j = 0; j <= k; j++) {
-    const double* vj = V + (long long)j * ld;
-    double s = 0;
-    for (int i = rg.x + threadIdx.x; i < rg.y; i += KT) s = fma(vj[i], w[i], s);
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) part[(long long)blockIdx.x * mp1 + j] = s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j0 = 0; j0 <= k; j0 += JG) {
+    const int nj = min(JG, k + 1 - j0);
+    const double* v0 = V + (long long)j0 * ld;
+    double acc[JG];
+#pragma unroll
+    for (int q = 0; q < JG; q++) acc[q] = 0.0;
+    for (int i = rg.x + threadIdx.x; i < rg.y; i += KT) {
+      const double wi = w[i];
+#pragma unroll
+      for (int q = 0; q < JG; q++)
+        if (q < nj) acc[q] = fma(v0[(long long)q * ld + i], wi, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < JG; q++) {
+      const double t = warp_sum(acc[q]);
+      if (lane == 0) sh[q][wid] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < nj) {
+      double t = 0;
+      for (int u = 0; u < KT / 32; u++) t += sh[threadIdx.x][u];
+      part[(long long)blockIdx.x * mp1 + j0 + threadIdx.x] = t;
+    }
+    __syncthreads();
   }
 }
 
@@ -89,7 +115,17 @@ __global__ void __launch_bounds__(KT) k_update_norm(const KGlob* __restrict__ G,
   double s2 = 0;
   for (int i = rg.x + threadIdx.x; i < rg.y; i += KT) {
     double wi = w[i];
-    for (int j = 0; j <= k; j++) wi = fma(-hs[j], V[(long long)j * ld + i], wi);
+    // JG loads issued together, the fmas in j order
+    for (int j0 = 0; j0 <= k; j0 += JG) {
+      const int nj = min(JG, k + 1 - j0);
+      const double* v0 = V + (long long)j0 * ld + i;
+      double vq[JG];
+#pragma unroll
+      for (int q = 0; q < JG; q++) vq[q] = q < nj ? v0[(long long)q * ld] : 0.0;
+#pragma unroll
+      for (int q = 0; q < JG; q++)
+        if (q < nj) wi = fma(-hs[j0 + q], vq[q], wi);
+    }
     w[i] = wi;
     s2 = fma(wi, wi, s2);
   }
@@ -422,9 +458,21 @@ void Krylov::build_graph(const Operator& op, cudaStream_t s) {
   graph_op = &op;
 }
 
+// PRBF_KRYLOV_EAGER=1 launches the iterations one kernel at a time instead of through the
+// graph's while node (same kernels, same results): profilers list the kernels of a
+// conditional graph body poorly, so a launch list of a solve is taken this way.
+static bool krylov_eager() {
+  static const bool e = [] {
+    const char* v = std::getenv("PRBF_KRYLOV_EAGER");
+    return v && v[0] == '1';
+  }();
+  return e;
+}
+
 std::vector<KResult> Krylov::solve(const Operator& op, const double* b, double* x, bool zero_x, double rtol,
                                    double abstol, double dtol, int maxit, bool use_graph, cudaStream_t s,
                                    const double* rnorm_ref, bool guard) {
+  if (krylov_eager()) use_graph = false;
   std::vector<KSeg> h0(nseg);
   for (int i = 0; i < nseg; i++) {
     KSeg& q = h0[i];

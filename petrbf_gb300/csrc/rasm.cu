@@ -1268,6 +1268,200 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
   }
 }
 
+// ---- FP32 apply with the factor, one warp per block -----------------------------------
+// The FP32 substitutions stream the packed factor twice and are bound by HBM, so no warp
+// of them may wait on another: each warp solves a whole block with its own y in shared
+// memory (no CTA barrier). Forward, 32-row panels from the top: lane i holds row p0+i of
+// the panel triangle in registers (its own 16-byte-aligned row segment), the panel's y is
+// solved by shuffles, and the rows below are updated four lanes per row, eight entries
+// each, four rows per lane in flight. Backward (L^T x = y over the whole block for basic
+// Schwarz, over the centre rows for the restricted form), 32-row panels aligned to
+// multiples of 32 from the bottom: lane i holds column P0+i of the panel triangle, and
+// the rows above are updated from the panel rows' contiguous segments L[P0+j][k], each
+// lane owning four consecutive k and keeping eight 16-byte loads in flight. Every access
+// stays inside the row it addresses: a segment starting at a multiple of 4 at or below
+// the row index lies inside the row's padded extent.
+constexpr int kTrwWarps = 4;
+
+template <int NV>
+__global__ void __launch_bounds__(kTrwWarps * 32) k_apply_trw(int ncell, const long long* __restrict__ boff,
+                                                             const int* __restrict__ cs, const int* __restrict__ idx,
+                                                             const long long* __restrict__ loff,
+                                                             const float* __restrict__ Lpack,
+                                                             const double* __restrict__ r, double* __restrict__ out,
+                                                             long long vs, const int* __restrict__ skip, int full,
+                                                             double* __restrict__ Y, long long ys, SegSkip seg,
+                                                             int ldy) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int c = blockIdx.x * kTrwWarps + wid;
+  if (c >= ncell || seg.cell_done(c)) return;
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  if (nb == 0) return;
+  float* y = (float*)smem_raw + (size_t)wid * NV * ldy;  // NV x ldy
+  const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
+  const int* id = idx + boff[c];
+  const float* L = Lpack + loff[c];
+  constexpr unsigned FULL = 0xffffffffu;
+  for (int j = lane; j < nb; j += 32) {
+    const int p = id[j < n1 ? nc + j : j - n1];
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v * ldy + j] = (float)r[v * vs + p];
+  }
+  __syncwarp();
+  // ---- forward: L y = r ----
+  const int sub = lane & 3, rw = lane >> 2;
+  for (int p0 = 0; p0 < nb; p0 += 32) {
+    const int np = min(32, nb - p0);
+    const bool act = lane < np;
+    float lrow[32];
+    {
+      const float4* Li = reinterpret_cast<const float4*>(L + rowoff<float>(p0 + lane) + p0);
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act && 4 * q <= lane) t = Li[q];
+        lrow[4 * q] = t.x;
+        lrow[4 * q + 1] = t.y;
+        lrow[4 * q + 2] = t.z;
+        lrow[4 * q + 3] = t.w;
+      }
+    }
+    float ri[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) ri[v] = act ? y[v * ldy + p0 + lane] : 0.f;
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if (j < np) {
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          if (lane == j) ri[v] *= lrow[j];  // reciprocal diagonal
+          const float yj = __shfl_sync(FULL, ri[v], j);
+          if (lane > j) ri[v] = fmaf(-lrow[j], yj, ri[v]);
+        }
+      }
+    }
+    if (act)
+#pragma unroll
+      for (int v = 0; v < NV; v++) y[v * ldy + p0 + lane] = ri[v];
+    // rows below the panel (only when it is full): y[i] -= L[i][p0 .. p0+32) . y[p0 ..]
+    if (p0 + 32 < nb) {
+      float ysv[NV][8];
+#pragma unroll
+      for (int v = 0; v < NV; v++)
+#pragma unroll
+        for (int q = 0; q < 8; q++) ysv[v][q] = __shfl_sync(FULL, ri[v], sub * 8 + q);
+      for (int i0 = p0 + 32; i0 < nb; i0 += 32) {
+        float4 lv[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = i0 + 8 * u + rw;
+          if (i < nb) {
+            const float4* Li = reinterpret_cast<const float4*>(L + rowoff<float>(i) + p0 + sub * 8);
+            lv[u][0] = Li[0];
+            lv[u][1] = Li[1];
+          } else {
+            lv[u][0] = lv[u][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = i0 + 8 * u + rw;
+          float acc[NV];
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            float a = lv[u][0].x * ysv[v][0];
+            a = fmaf(lv[u][0].y, ysv[v][1], a);
+            a = fmaf(lv[u][0].z, ysv[v][2], a);
+            a = fmaf(lv[u][0].w, ysv[v][3], a);
+            a = fmaf(lv[u][1].x, ysv[v][4], a);
+            a = fmaf(lv[u][1].y, ysv[v][5], a);
+            a = fmaf(lv[u][1].z, ysv[v][6], a);
+            a = fmaf(lv[u][1].w, ysv[v][7], a);
+            a += __shfl_xor_sync(FULL, a, 1);
+            a += __shfl_xor_sync(FULL, a, 2);
+            acc[v] = a;
+          }
+          if (sub == 0 && i < nb)
+#pragma unroll
+            for (int v = 0; v < NV; v++) y[v * ldy + i] -= acc[v];
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // ---- backward: L22^T x2 = y2 over rows [b0, nb) ----
+  const int b0 = full ? 0 : n1;
+  for (int pt = (nb - 1) & ~31; pt >= 0 && pt + 32 > b0; pt -= 32) {
+    const int P0 = max(pt, b0), np = min(nb, pt + 32) - P0;
+    float lcol[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) lcol[j] = (j < np && lane <= j) ? L[rowoff<float>(P0 + j) + P0 + lane] : 0.f;
+    float xi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) xi[v] = lane < np ? y[v * ldy + P0 + lane] : 0.f;
+#pragma unroll
+    for (int j = 31; j >= 0; j--) {
+      if (j < np) {
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          if (lane == j) xi[v] *= lcol[j];
+          const float xj = __shfl_sync(FULL, xi[v], j);
+          if (lane < j) xi[v] = fmaf(-lcol[j], xj, xi[v]);
+        }
+      }
+    }
+    if (lane < np)
+#pragma unroll
+      for (int v = 0; v < NV; v++) y[v * ldy + P0 + lane] = xi[v];
+    __syncwarp();
+    // rows above the panel: y2[k] -= sum_j L[P0+j][k] x_j, b0 <= k < P0 (k4 starts at b0
+    // rounded down to 4; the entries outside [b0, P0) are read but not applied)
+    for (int k4 = (b0 & ~3) + 4 * lane; k4 < P0; k4 += 128) {
+      float acc[NV][4];
+#pragma unroll
+      for (int v = 0; v < NV; v++) acc[v][0] = acc[v][1] = acc[v][2] = acc[v][3] = 0.f;
+      for (int j0 = 0; j0 < np; j0 += 8) {
+        float4 lv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          lv[u] = j0 + u < np ? *reinterpret_cast<const float4*>(L + rowoff<float>(P0 + j0 + u) + k4)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          if (j0 + u < np) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+              const float xj = y[v * ldy + P0 + j0 + u];
+              acc[v][0] = fmaf(lv[u].x, xj, acc[v][0]);
+              acc[v][1] = fmaf(lv[u].y, xj, acc[v][1]);
+              acc[v][2] = fmaf(lv[u].z, xj, acc[v][2]);
+              acc[v][3] = fmaf(lv[u].w, xj, acc[v][3]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < NV; v++)
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+          if (k4 + e >= b0 && k4 + e < P0) y[v * ldy + k4 + e] -= acc[v][e];
+    }
+    __syncwarp();
+  }
+  if (full) {
+    double* Yc = Y + boff[c];
+    for (int j = lane; j < nb; j += 32)
+#pragma unroll
+      for (int v = 0; v < NV; v++) Yc[v * ys + (j < n1 ? nc + j : j - n1)] = (double)y[v * ldy + j];
+  } else {
+    for (int i = lane; i < nc; i += 32)
+#pragma unroll
+      for (int v = 0; v < NV; v++) out[v * vs + cs[c] + i] = (double)y[v * ldy + n1 + i];
+  }
+}
+
 // basic Schwarz: out[i] = sum of the slots of point i (ascending slot = ascending block)
 __global__ void k_asm_gather(int n, int nv, const long long* __restrict__ inv_off,
                              const long long* __restrict__ inv_slot, const double* __restrict__ Y, long long ys,
@@ -1558,42 +1752,76 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
 }
 
 namespace {
+int trw_ldy(const RasmPlan& R) { return (std::max(R.max_nb, 1) + 3) & ~3; }
+
 template <class T>
 void apply_tri_nv(const RasmPlan& R, const T* Lp, const int* cs, const double* r, double* out, long long vs, int nv,
                   cudaStream_t s, const int* skip) {
-  const size_t sm = (size_t)nv * R.max_nb * sizeof(T);
   const int full = R.basic ? 1 : 0;
-  switch (nv) {
-    case 1:
-      k_apply_tri<T, 1><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
-                                                 skip, full, R.Y.get(), R.nslot, R.seg);
-      break;
-    case 2:
-      k_apply_tri<T, 2><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
-                                                 skip, full, R.Y.get(), R.nslot, R.seg);
-      break;
-    case 3:
-      k_apply_tri<T, 3><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
-                                                 skip, full, R.Y.get(), R.nslot, R.seg);
-      break;
-    default:
-      k_apply_tri<T, 4><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out, vs,
-                                                 skip, full, R.Y.get(), R.nslot, R.seg);
-      break;
+  if constexpr (std::is_same<T, float>::value) {
+    const int ldy = trw_ldy(R);
+    const size_t sm = (size_t)kTrwWarps * nv * ldy * sizeof(float);
+    const int grid = ceil_div(R.ncell, kTrwWarps);
+    switch (nv) {
+      case 1:
+        k_apply_trw<1><<<grid, kTrwWarps * 32, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r,
+                                                        out, vs, skip, full, R.Y.get(), R.nslot, R.seg, ldy);
+        break;
+      case 2:
+        k_apply_trw<2><<<grid, kTrwWarps * 32, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r,
+                                                        out, vs, skip, full, R.Y.get(), R.nslot, R.seg, ldy);
+        break;
+      case 3:
+        k_apply_trw<3><<<grid, kTrwWarps * 32, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r,
+                                                        out, vs, skip, full, R.Y.get(), R.nslot, R.seg, ldy);
+        break;
+      default:
+        k_apply_trw<4><<<grid, kTrwWarps * 32, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r,
+                                                        out, vs, skip, full, R.Y.get(), R.nslot, R.seg, ldy);
+        break;
+    }
+  } else {
+    const size_t sm = (size_t)nv * R.max_nb * sizeof(T);
+    switch (nv) {
+      case 1:
+        k_apply_tri<T, 1><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+        break;
+      case 2:
+        k_apply_tri<T, 2><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+        break;
+      case 3:
+        k_apply_tri<T, 3><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+        break;
+      default:
+        k_apply_tri<T, 4><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+        break;
+    }
   }
   PRBF_CHECK_LAUNCH();
 }
 
 template <class T>
 void set_tri_smem(const RasmPlan& R) {
-  const size_t st = sizeof(T) * 32 * 33;
   for (int nv = 1; nv <= std::max(1, std::min(4, R.max_nv)); nv++) {
-    size_t sm = (size_t)nv * std::max(R.max_nb, 1) * sizeof(T);
-    if (sm + st > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
-    const void* f = nv == 1 ? (const void*)k_apply_tri<T, 1>
-                            : nv == 2 ? (const void*)k_apply_tri<T, 2>
-                                      : nv == 3 ? (const void*)k_apply_tri<T, 3> : (const void*)k_apply_tri<T, 4>;
-    PRBF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    size_t sm;
+    const void* f;
+    if constexpr (std::is_same<T, float>::value) {
+      sm = (size_t)kTrwWarps * nv * trw_ldy(R) * sizeof(float);
+      f = nv == 1 ? (const void*)k_apply_trw<1>
+                  : nv == 2 ? (const void*)k_apply_trw<2> : nv == 3 ? (const void*)k_apply_trw<3> : (const void*)k_apply_trw<4>;
+    } else {
+      sm = (size_t)nv * std::max(R.max_nb, 1) * sizeof(T) + sizeof(T) * 32 * 33;
+      f = nv == 1 ? (const void*)k_apply_tri<T, 1>
+                  : nv == 2 ? (const void*)k_apply_tri<T, 2>
+                            : nv == 3 ? (const void*)k_apply_tri<T, 3> : (const void*)k_apply_tri<T, 4>;
+    }
+    if (sm > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the apply kernel's shared memory");
+    PRBF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(std::is_same<T, float>::value ? sm : sm - sizeof(T) * 32 * 33)));
   }
 }
 }  // namespace
