@@ -775,7 +775,35 @@ def run_case(name):
         with Context(dim=3, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
                      sigma_trunc=p.sigma_trunc, precision="mixed", rtol=1e-12, pc="asm") as c:
             _, st = c.interpolate(p.x, p.y, p.z, p.f)
-        print("its", st.its, "outer", st.outer_its, "solve_ms", st.t_solve_ms, "setup_ms", st.t_setup_ms)
+        print("its", st.its, "outer", st.outer_its, "solve_ms", st.t_solve_ms, "setup_ms", st.t_setup_ms,
+              "reason", st.reason, "true_rel_resid", st.true_rel_resid)
+    elif name == "mixed2d":  # the 2D mixed solve: 2000 x 2000 jittered lattice (4x10^6 points), to 1e-13
+        p = W.lamb_oseen_2d(2000, jitter=0.25, seed=12345)
+        with Context(dim=2, sigma=p.sigma, nsigma_box=8, sigma_buffer=24, sigma_trunc=24, precision="mixed",
+                     rtol=1e-13) as c:
+            _, st = c.interpolate(p.x, p.y, None, p.f)
+        print("its", st.its, "outer", st.outer_its, "solve_ms", st.t_solve_ms, "setup_ms", st.t_setup_ms,
+              "reason", st.reason, "true_rel_resid", st.true_rel_resid)
+    elif name == "time3d":  # CUDA-event times of the 3D single-vector products, 128^3 vortex-ring lattice
+        p = W.vortex_ring_3d(m=128)
+        c = Context(dim=3, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+                    sigma_trunc=p.sigma_trunc)
+        c.matvec_setup(p.x, p.y, p.z)
+        v = torch.randn(p.n, dtype=torch.float64, device="cuda")
+        o = torch.empty_like(v)
+        stream = torch.cuda.ExternalStream(c.stream)
+        for fp32 in (False, True):
+            for _ in range(3):
+                c.matvec_dev(v.data_ptr(), o.data_ptr(), cell_order=True, fp32=fp32)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(5):
+                c.matvec_dev(v.data_ptr(), o.data_ptr(), cell_order=True, fp32=fp32)
+            e1.record(stream)
+            c.synchronize()
+            print("fp32" if fp32 else "fp64", "ms per product %.3f" % (e0.elapsed_time(e1) / 5),
+                  "Gpairs/s %.1f" % (c.matvec_info()["pairs"] / (e0.elapsed_time(e1) / 5 * 1e-3) / 1e9))
+        c.close()
     elif name == "seam_2d":  # the gpumatmult seam on the packed arrays of a 10^6-point lattice
         run_seam_case()
         return

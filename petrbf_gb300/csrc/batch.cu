@@ -442,7 +442,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   } else {
     // FP64 iterative refinement of every problem: r = f - A g (FP64 sums, skipping the
     // problems that have stopped), stop test on ||r|| <= rtol ||f||, then A d = r by GMRES
-    // with FP32 operators to 1e-6 and g += d in FP64.
+    // with FP32 operators to kInnerRtol and g += d in FP64.
     B.odone.reserve(nprob);
     PRBF_CUDA(cudaMemsetAsync(B.odone.get(), 0, sizeof(int) * nprob, c.stream));
     SegSkip oseg;
@@ -509,7 +509,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
       PRBF_CUDA(cudaMemsetAsync(B.d.get(), 0, sizeof(double) * ldv, c.stream));
       const int budget_its = std::min(p.max_it - inner_max, 4 * p.restart);
       std::vector<KResult> in =
-          B.kry.solve(B.op32, B.r.get(), B.d.get(), true, 1e-6, 0.0, 1e10, budget_its, true, c.stream);
+          B.kry.solve(B.op32, B.r.get(), B.d.get(), true, kInnerRtol, 0.0, 1e10, budget_its, true, c.stream);
       int step = 0;
       bool progress = false;
       for (int i = 0; i < nprob; i++) {

@@ -263,14 +263,23 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             }
           }
         }
+        // the four target sums over the warp by a reduce-scatter butterfly (6 adds per
+        // vector instead of 4 x 5; FP64 adds run on the narrow FP64 pipe): lane 8 k ends
+        // with target k
+        static_assert(kGroup == 4, "reduce-scatter of four sums");
+        const bool h16 = lane & 16, h8 = lane & 8;
+        const int t = gi * kGroup + (lane >> 3);
 #pragma unroll
-        for (int k = 0; k < kGroup; k++) {
-          int t = gi * kGroup + k;
-#pragma unroll
-          for (int v = 0; v < NV; v++) {
-            T s = warp_sum(a[k][v]);
-            if (lane == 0 && t < nt) acc[v * kTileT + t] += s;
-          }
+        for (int v = 0; v < NV; v++) {
+          T k0 = h16 ? a[2][v] : a[0][v], k1 = h16 ? a[3][v] : a[1][v];
+          k0 += __shfl_xor_sync(0xffffffffu, h16 ? a[0][v] : a[2][v], 16);
+          k1 += __shfl_xor_sync(0xffffffffu, h16 ? a[1][v] : a[3][v], 16);
+          T kp = h8 ? k1 : k0;
+          kp += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 4);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 2);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 1);
+          if ((lane & 7) == 0 && t < nt) acc[v * kTileT + t] += kp;
         }
       }
       ncomp = 0;
@@ -584,14 +593,22 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
             for (int v = 0; v < NV; v++) a[k][v] = fmaf(gj[v], e, a[k][v]);
           }
         }
+        // the four target sums over the warp by a butterfly that halves the values each lane
+        // carries (6 shuffles per vector instead of 4 x 5): lane 8 k ends with target k
+        static_assert(kGroup == 4, "reduce-scatter of four sums");
+        const bool h16 = lane & 16, h8 = lane & 8;
+        const int t = gi * kGroup + (lane >> 3);
 #pragma unroll
-        for (int k = 0; k < kGroup; k++) {
-          int t = gi * kGroup + k;
-#pragma unroll
-          for (int v = 0; v < NV; v++) {
-            float sm = warp_sum(a[k][v]);
-            if (lane == 0 && t < nt) acc[v * kTileT + t] += sm;
-          }
+        for (int v = 0; v < NV; v++) {
+          float k0 = h16 ? a[2][v] : a[0][v], k1 = h16 ? a[3][v] : a[1][v];
+          k0 += __shfl_xor_sync(0xffffffffu, h16 ? a[0][v] : a[2][v], 16);
+          k1 += __shfl_xor_sync(0xffffffffu, h16 ? a[1][v] : a[3][v], 16);
+          float kp = h8 ? k1 : k0;
+          kp += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 4);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 2);
+          kp += __shfl_xor_sync(0xffffffffu, kp, 1);
+          if ((lane & 7) == 0 && t < nt) acc[v * kTileT + t] += kp;
         }
       }
       ncomp = 0;

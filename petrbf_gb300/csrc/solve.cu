@@ -271,7 +271,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
       }
       PRBF_CUDA(cudaMemsetAsync(S.d.get(), 0, sizeof(double) * len_all, c.stream));
       int budget_its = std::min(p.max_it - inner_max, 4 * p.restart);
-      std::vector<KResult> in = S.kry.solve(S.op32, S.r.get(), S.d.get(), true, 1e-6, 0.0, 1e10, budget_its, true,
+      std::vector<KResult> in = S.kry.solve(S.op32, S.r.get(), S.d.get(), true, kInnerRtol, 0.0, 1e10, budget_its, true,
                                             c.stream);
       int step = 0;
       bool progress = false;
