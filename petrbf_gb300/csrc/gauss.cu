@@ -468,10 +468,15 @@ struct LayoutF {
   static constexpr int RC = DIM == 3 ? 384 : 512;      // staged sources per fill
   static constexpr int kComp = DIM == 3 ? 768 : 1024;  // compacted sources (>= RC)
   static_assert(kComp >= RC, "a fill must fit the compaction buffer");
+  // a compacted source is one float4 (coordinates, then weights) and, when NF > 4, a
+  // float2 or float4 with the remaining weights: two shared loads per source in the pair loop
+  static constexpr int NX = NF <= 4 ? 0 : (NF <= 6 ? 2 : 4);
+  static_assert(NF <= 8, "at most four weight vectors");
   static constexpr size_t rawf = 0;
   static constexpr size_t rawm = align16(rawf + sizeof(float) * NF * RC);
-  static constexpr size_t comp = align16(rawm + sizeof(unsigned long long) * RC);
-  static constexpr size_t tgt = align16(comp + sizeof(float) * NF * kComp);
+  static constexpr size_t comp = align16(rawm + sizeof(unsigned long long) * RC);  // float4 x kComp
+  static constexpr size_t compx = align16(comp + sizeof(float) * 4 * kComp);        // NX floats x kComp
+  static constexpr size_t tgt = align16(compx + sizeof(float) * NX * kComp);
   static constexpr size_t acc = align16(tgt + sizeof(float) * DIM * kTileT);
   static constexpr size_t pieces = align16(acc + sizeof(float) * NV * kTileT);
   static constexpr size_t bar = align16(pieces + sizeof(Piece) * kMaxPieces);
@@ -481,7 +486,7 @@ struct LayoutF {
 // BATCH: as k_gauss (the item's cell indexes a concatenation of grids); the source data
 // of each problem were built with its own grid and scale.
 template <int DIM, int NV, bool BATCH>
-__global__ void __launch_bounds__(kThreads) k_gauss_f32m(
+__global__ void __launch_bounds__(kThreads, 6) k_gauss_f32m(
     Grid g0, const Grid* __restrict__ grids, const int* __restrict__ cprob, SegSkip seg,
     const int2* __restrict__ items, int nitems, const double* __restrict__ tx, const double* __restrict__ ty,
     const double* __restrict__ tz, const int* __restrict__ cs_t, const float* __restrict__ su,
@@ -490,13 +495,15 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
     long long vs_w, double scale0, double norm0, unsigned* err, const int* __restrict__ skip) {
   if (skip && *skip) return;
   using Lay = LayoutF<DIM, NV>;
-  constexpr int NF = Lay::NF, KC = Lay::kComp, RC = Lay::RC;
+  constexpr int NF = Lay::NF, RC = Lay::RC, NX = Lay::NX;
   extern __shared__ __align__(16) unsigned char smem[];
   float* rawf = (float*)(smem + Lay::rawf);                           // NF x RC
   unsigned long long* rawm = (unsigned long long*)(smem + Lay::rawm);  // RC
-  float* comp = (float*)(smem + Lay::comp);                           // NF x KC
+  float4* comp = (float4*)(smem + Lay::comp);                         // KC
+  float* compx = (float*)(smem + Lay::compx);                         // KC x NX
   float* tgt = (float*)(smem + Lay::tgt);                             // DIM x kTileT
   float* acc = (float*)(smem + Lay::acc);                             // NV x kTileT
+  constexpr int KC = Lay::kComp;
   Piece* pieces = (Piece*)(smem + Lay::pieces);
   uint64_t* bar = (uint64_t*)(smem + Lay::bar);
   __shared__ int s_wsum[kWarps];
@@ -576,10 +583,29 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
           for (int v = 0; v < NV; v++) a[k][v] = 0.f;
         }
         for (int j = lane; j < ncomp; j += 32) {
-          const float cu = comp[j], cv = comp[KC + j], cw = DIM == 3 ? comp[2 * KC + j] : 0.f;
+          float rec[4 + NX];
+          {
+            const float4 c4 = comp[j];
+            rec[0] = c4.x;
+            rec[1] = c4.y;
+            rec[2] = c4.z;
+            rec[3] = c4.w;
+            if constexpr (NX == 2) {
+              const float2 c2 = reinterpret_cast<const float2*>(compx)[j];
+              rec[4] = c2.x;
+              rec[5] = c2.y;
+            } else if constexpr (NX == 4) {
+              const float4 c4b = reinterpret_cast<const float4*>(compx)[j];
+              rec[4] = c4b.x;
+              rec[5] = c4b.y;
+              rec[6] = c4b.z;
+              rec[7] = c4b.w;
+            }
+          }
+          const float cu = rec[0], cv = rec[1], cw = DIM == 3 ? rec[2] : 0.f;
           float gj[NV];
 #pragma unroll
-          for (int v = 0; v < NV; v++) gj[v] = comp[(DIM + v) * KC + j];
+          for (int v = 0; v < NV; v++) gj[v] = rec[DIM + v];
 #pragma unroll
           for (int k = 0; k < kGroup; k++) {
             float du = tu[k] - cu, dv = tv[k] - cv;
@@ -728,11 +754,19 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
           if (in) {
             int pos = ncomp + pre + __popc(bal & ((1u << lane) - 1u));
             const int jy = (int)(m >> kMaskCellY);
-            comp[pos] = rawf[ro] + offx;
-            comp[KC + pos] = rawf[RC + ro] + (float)(jy - iy) * boxs;
-            if (DIM == 3) comp[2 * KC + pos] = rawf[2 * RC + ro] + offz;
+            float rec[4 + NX];
 #pragma unroll
-            for (int v = 0; v < NV; v++) comp[(DIM + v) * KC + pos] = rawf[(DIM + v) * RC + ro];
+            for (int q = 0; q < 4 + NX; q++) rec[q] = 0.f;
+            rec[0] = rawf[ro] + offx;
+            rec[1] = rawf[RC + ro] + (float)(jy - iy) * boxs;
+            if (DIM == 3) rec[2] = rawf[2 * RC + ro] + offz;
+#pragma unroll
+            for (int v = 0; v < NV; v++) rec[DIM + v] = rawf[(DIM + v) * RC + ro];
+            comp[pos] = make_float4(rec[0], rec[1], rec[2], rec[3]);
+            if constexpr (NX == 2)
+              reinterpret_cast<float2*>(compx)[pos] = make_float2(rec[4], rec[5]);
+            else if constexpr (NX == 4)
+              reinterpret_cast<float4*>(compx)[pos] = make_float4(rec[4], rec[5], rec[6], rec[7]);
           }
           ncomp += tot;
           __syncthreads();
@@ -743,7 +777,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss_f32m(
     __syncthreads();
     for (int t = tid; t < nt; t += kThreads)
 #pragma unroll
-      for (int v = 0; v < NV; v++) w[v * vs_w + t0 + t] = (double)acc[v * kTileT + t] * norm;
+      for (int v = 0; v < NV; v++)
+        w[v * vs_w + t0 + t] = (double)acc[v * kTileT + t] * norm;
   }
 }
 

@@ -511,13 +511,15 @@ __device__ __forceinline__ void tile_range(int t, int n1, int nb, int kc1, int& 
   }
 }
 
-// Packed factor rows: row i holds L[i][0..i] padded to a multiple of PackA<T> elements
-// (16 bytes), so every row starts 16-byte aligned and 8-element segments at multiples of 8
-// load as vectors. rowoff(i) = sum_{r<i} A ceil((r+1)/A) = A (A q(q+1)/2 + rr (q+1)),
+// Packed factor rows: row i holds L[i][0..i] padded to a multiple of PackA<T> elements, so
+// every row starts aligned and 8-element segments at multiples of 8 load as vectors. FP32
+// rows are padded to 32 bytes, the DRAM sector: the substitutions stream 128-byte row
+// segments, which then cover four whole sectors instead of straddling five. FP64 rows
+// are padded to 16 bytes. rowoff(i) = sum_{r<i} A ceil((r+1)/A) = A (A q(q+1)/2 + rr (q+1)),
 // q = i / A, rr = i % A.
 template <class T>
 struct PackA {
-  static constexpr int v = 16 / sizeof(T);
+  static constexpr int v = std::is_same<T, float>::value ? 8 : 2;
 };
 template <class T>
 __host__ __device__ __forceinline__ long long rowoff(long long i) {

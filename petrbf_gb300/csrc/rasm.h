@@ -18,7 +18,7 @@ struct RasmPlan {
   DevBuf<int> idx;            // buffer lists (sorted positions), centre first
   DevBuf<long long> soff;     // S_c offsets per cell (n_c * n_b each)
   bool factor = false;        // apply by triangular solves with the kept factor (FP64 form)
-  DevBuf<long long> loff;     // packed-factor offsets per cell (rows padded to 16 bytes)
+  DevBuf<long long> loff;     // packed-factor offsets per cell (rows padded to 32 bytes FP32, 16 FP64)
   DevBuf<double> L64;         // packed Cholesky factors (FP64 factor form), rows in block order
   DevBuf<float> L32;          // packed Cholesky factors (FP32 factor form)
   DevBuf<float> S32;          // S_c (FP32 inverse-rows form)
