@@ -53,15 +53,25 @@ struct ExpTab {
   static constexpr int bits = BIG ? 10 : 8, n = 1 << bits, poly = BIG ? 4 : 5;
 };
 template <int DIM, int NV>
-struct UseBigTab {
+struct UseBigTabSym {  // the symmetric sum keeps the 256-entry table in 3D (two CTAs per SM)
   static constexpr bool v = DIM == 2 && NV <= 2;
+};
+template <int DIM, int NV>
+struct UseBigTab {
+  // 2D one or two vectors; 3D every vector count of the one-sided sum (its staging buffers
+  // are sized so that the large table still leaves two CTAs per SM, Cfg)
+  static constexpr bool v = DIM == 2 ? NV <= 2 : true;
 };
 __device__ double d_tab_big[ExpTab<true>::n * ExpTab<true>::poly];  // copied into shared memory by each CTA
 __device__ double d_tab_small[ExpTab<false>::n * ExpTab<false>::poly];
 
 template <int DIM, bool F32, int NV>
 struct Cfg {
-  static constexpr int kComp = (NV > 1 ? 1024 : (F32 ? 2048 : (DIM == 3 ? 1536 : 2048)));
+  // 3D FP64: smaller fills and compaction buffers, so that the 1024-entry exp table (one
+  // FP64 instruction per pair fewer than the 256-entry quartic) fits two CTAs per SM
+  static constexpr bool k3d64 = DIM == 3 && !F32;
+  static constexpr int kComp = k3d64 ? (NV > 1 ? 768 : 1024) : (NV > 1 ? 1024 : 2048);
+  static constexpr int kRaw = k3d64 ? 512 : kRawCap;
   using T = typename std::conditional<F32, float, double>::type;
 };
 
@@ -79,7 +89,7 @@ struct Layout {
   using T = typename Cfg<DIM, F32, NV>::T;
   static constexpr int NA = DIM + NV;
   static constexpr size_t raw = 0;
-  static constexpr size_t comp = align16(raw + sizeof(double) * NA * kRawCap);
+  static constexpr size_t comp = align16(raw + sizeof(double) * NA * Cfg<DIM, F32, NV>::kRaw);
   static constexpr size_t tgt = align16(comp + sizeof(T) * NA * Cfg<DIM, F32, NV>::kComp);
   static constexpr size_t acc = align16(tgt + sizeof(T) * DIM * kTileT);
   static constexpr size_t tab = align16(acc + sizeof(T) * NV * kTileT);
@@ -120,8 +130,14 @@ __host__ __device__ inline SumConsts sum_consts(double sigma, bool f32, int ntab
 // plan sorts by decreasing cost): with one CTA per item this is the plain launch, with
 // fewer CTAs it is a persistent kernel. BATCH: the item's cell indexes a concatenation of
 // grids (cell -> problem -> Grid with its first global cell and sigma).
+// FP64 forms run two CTAs per SM (shared memory): registers are not the limit there
+template <bool F32>
+struct GaussMinBlocks {
+  static constexpr int v = F32 ? 1 : 2;
+};
+
 template <int DIM, bool F32, int NV, bool BATCH>
-__global__ void __launch_bounds__(kThreads) k_gauss(
+__global__ void __launch_bounds__(kThreads, GaussMinBlocks<F32>::v) k_gauss(
     Grid g0, const Grid* __restrict__ grids, const int* __restrict__ cprob, const int2* __restrict__ items, int nitems,
     const double* __restrict__ tx, const double* __restrict__ ty, const double* __restrict__ tz,
     const int* __restrict__ cs_t, const double* __restrict__ sx, const double* __restrict__ sy,
@@ -133,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
   constexpr int NA = DIM + NV;  // staged arrays: coordinates + weights
   extern __shared__ __align__(16) unsigned char smem[];
   const Layout<DIM, F32, NV> lay;
-  double* raw = (double*)(smem + lay.raw);      // NA x kRawCap (FP64, as stored in HBM)
+  double* raw = (double*)(smem + lay.raw);      // NA x C::kRaw (FP64, as stored in HBM)
   T* comp = (T*)(smem + lay.comp);              // NA x kComp (compacted truncation set)
   T* tgt = (T*)(smem + lay.tgt);                // DIM x kTileT
   T* acc = (T*)(smem + lay.acc);                // NV x kTileT
@@ -291,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
         int r = s_cursor[0], p = s_cursor[1];
         int used = 0, np = 0, valid = 0;
         unsigned bytes = 0;
-        while (r < nranges && np < kMaxPieces && kRawCap - used >= 4) {
+        while (r < nranges && np < kMaxPieces && C::kRaw - used >= 4) {
           int jx = jx0 + r % ncolx, jz = jz0 + r / ncolx;
           // (the FP64 kernel keeps no range table: with three weight vectors two CTAs per SM
           // fill the shared memory to within a few hundred bytes)
@@ -303,7 +319,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             continue;
           }
           int s_al = s & ~1;
-          int room = (kRawCap - used) & ~1;
+          int room = (C::kRaw - used) & ~1;
           int e_al = min((b + 1) & ~1, s_al + room);
           int e = min(b, e_al);
           pieces[np].raw_off = used + (s - s_al);
@@ -333,11 +349,11 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             int len = ((s + pieces[q].count + 1) & ~1) - s_al;
             int dst = pieces[q].raw_off - (s - s_al);
             bulk_g2s(raw + dst, sx + s_al, len * 8u, bar);
-            bulk_g2s(raw + kRawCap + dst, sy + s_al, len * 8u, bar);
-            if (DIM == 3) bulk_g2s(raw + 2 * kRawCap + dst, sz + s_al, len * 8u, bar);
+            bulk_g2s(raw + C::kRaw + dst, sy + s_al, len * 8u, bar);
+            if (DIM == 3) bulk_g2s(raw + 2 * C::kRaw + dst, sz + s_al, len * 8u, bar);
 #pragma unroll
             for (int v = 0; v < NV; v++)
-              bulk_g2s(raw + (DIM + v) * kRawCap + dst, sg + v * vstride + s_al, len * 8u, bar);
+              bulk_g2s(raw + (DIM + v) * C::kRaw + dst, sg + v * vstride + s_al, len * 8u, bar);
           }
         }
       }
@@ -373,8 +389,8 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             int j = pc.gstart + e;
             ro = pc.raw_off + e;
             vx = raw[ro];
-            vy = raw[kRawCap + ro];
-            if (DIM == 3) vz = raw[2 * kRawCap + ro];
+            vy = raw[C::kRaw + ro];
+            if (DIM == 3) vz = raw[2 * C::kRaw + ro];
             // centre cell unconditionally (2d/get_trunc.h:31-39), neighbours by the box test
             // fabs(xj - xc) < trunc_length && ... (2d/get_trunc.h:63; 3d/get_trunc.h:70-72)
             bool boxin = fabs(vx - xc) < L && fabs(vy - yc) < L;
@@ -397,7 +413,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss(
             comp[C::kComp + pos] = (T)((vy - yc) * scale);
             if (DIM == 3) comp[2 * C::kComp + pos] = (T)((vz - zc) * scale);
 #pragma unroll
-            for (int v = 0; v < NV; v++) comp[(DIM + v) * C::kComp + pos] = (T)raw[(DIM + v) * kRawCap + ro];
+            for (int v = 0; v < NV; v++) comp[(DIM + v) * C::kComp + pos] = (T)raw[(DIM + v) * C::kRaw + ro];
           }
           ncomp += tot;
           __syncthreads();
@@ -808,7 +824,7 @@ template <int DIM, int NV>
 struct LayoutS {
   static constexpr int KC = NV == 1 ? 1024 : 768;  // compacted sources
   static constexpr int NA = DIM + NV + 1;  // staged arrays: coordinates, weights, cell-y word
-  using ET = ExpTab<UseBigTab<DIM, NV>::v>;
+  using ET = ExpTab<UseBigTabSym<DIM, NV>::v>;
   static constexpr size_t raw = 0;                                                     // NA x RC
   static constexpr size_t comp = align16(raw + sizeof(double) * NA * kSymRC);           // (DIM+NV) x KC
   static constexpr size_t code = align16(comp + sizeof(double) * (DIM + NV) * KC);      // KC
@@ -900,7 +916,7 @@ __global__ void __launch_bounds__(kThreads) k_gauss_sym(
   __shared__ unsigned long long s_tor;
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (UseBigTab<DIM, NV>::v ? d_tab_big : d_tab_small)[i];
+  for (int i = tid; i < ET::n * ET::poly; i += kThreads) tab[i] = (UseBigTabSym<DIM, NV>::v ? d_tab_big : d_tab_small)[i];
   if (tid == 0) mbar_init(bar, 1);
   unsigned phase = 0;
   const int G = gridDim.x;
