@@ -58,6 +58,20 @@ enum {
   PRBF_PC_ASM = 1    /* basic: every block's whole solution is added back (symmetric B) */
 };
 
+/* What the FP64 set-up does with a block whose Cholesky meets a non-positive pivot (a
+ * near-singular block: clustered or duplicated points). The reference factors every block
+ * by PETSc's dense LU with partial pivoting (-sub_pc_type lu, 2d/Makefile:7), which solves
+ * such a block unshifted and stops with an error on an exactly zero pivot.
+ * PRBF_FALLBACK_LU does the same for those blocks (LU with partial pivoting of the
+ * library's block; a zero pivot returns PRBF_ERR_FACTOR); PRBF_FALLBACK_SHIFT (default)
+ * refactors them with a diagonal shift of 1e-12, then 1e-9, relative to the unit
+ * diagonal, so that duplicated points still give a usable preconditioner. The FP32
+ * set-up of the mixed form always shifts (its refinement falls back to the FP64 form). */
+enum {
+  PRBF_FALLBACK_SHIFT = 0,
+  PRBF_FALLBACK_LU = 1
+};
+
 /* Flags of prbf_matvec_dev. */
 enum {
   PRBF_ORDER_CALLER = 0, /* vectors in the order the points were given */
@@ -80,6 +94,7 @@ typedef struct {
   int guess;         /* PRBF_GUESS_* */
   int device;        /* CUDA device ordinal (default 0) */
   int pc_type;       /* PRBF_PC_* (default PRBF_PC_RASM) */
+  int block_fallback; /* PRBF_FALLBACK_* (default PRBF_FALLBACK_SHIFT) */
 } prbf_params;
 
 typedef struct {
@@ -88,7 +103,7 @@ typedef struct {
   int outer_its;            /* iterative-refinement steps (mixed) */
   int ncell;                /* cells of the grid */
   int max_block;            /* largest RASM subdomain */
-  int nblocks_fallback;     /* blocks that needed a diagonal shift or FP64 refactor */
+  int nblocks_fallback;     /* blocks that needed a diagonal shift, an LU or an FP64 refactor */
   double rnorm0, rnorm;     /* first and last preconditioned residual norm */
   double true_rel_resid;    /* ||f - A g||_2 / ||f||_2 in FP64 after the solve */
   double t_sort_ms;         /* cell-list build */
@@ -195,7 +210,8 @@ int prbf_pc_buffer_lists(prbf_ctx* ctx, long long* off_out, int* idx_out);
  * (neighbour points -- buffer entries nc .. nb-1 -- first, then the centre points), before
  * any diagonal shift; L_out (nb (nb + 1) / 2, nullable, FP64 set-up only) the packed factor
  * as the apply reads it: row i holds L[i][0..i-1] and then 1 / L[i][i], where L L^T = A_c in
- * that order. Returns PRBF_ERR_STATE for L_out after a mixed-precision set-up. */
+ * that order. Returns PRBF_ERR_STATE for L_out after a mixed-precision set-up, or for a
+ * block that PRBF_FALLBACK_LU factored by LU. */
 int prbf_pc_block(prbf_ctx* ctx, int cell, int* nb_out, int* nc_out, double* K_out, double* L_out);
 
 /* ---- batches of independent problems (no reference counterpart: the reference solves

@@ -200,13 +200,14 @@ def gpu_block(g, idx, nc, xs, ys, zs):
     return np.tril(K) + np.tril(K, -1).T
 
 
-FACTORS = {"lu": 0, "chol": 1}
+FACTORS = {"lu": 0, "chol": 1, "chol_lu": 2}
 
 
 class Rasm:
     """Restricted (or, with basic=True, basic) additive Schwarz. factor "lu": dense LU with
     partial pivoting (PETSc's, the reference's); "chol": the GPU library's block arithmetic
-    restated (table exp, neighbours first, ordered Cholesky, its substitution order)."""
+    restated (table exp, neighbours first, ordered Cholesky, its substitution order);
+    "chol_lu": the same with the GPU's LU fallback for blocks whose Cholesky fails."""
 
     def __init__(self, g, xs, ys, zs, cs, basic=False, factor="lu"):
         self.g = g
@@ -279,7 +280,8 @@ def rbf_interpolation(x, y, z, f, sigma, nsigma_box, sigma_buffer, sigma_trunc, 
                                        _d(f), sigma, nsigma_box, sigma_buffer, sigma_trunc,
                                        rtol, restart, max_it, _d(gout), ctypes.byref(its),
                                        ctypes.byref(reason),
-                                       (1 if pc == "asm" else 0) | (2 * FACTORS[factor]) | (4 if texp else 0)
+                                       (1 if pc == "asm" else 0) | (2 if factor != "lu" else 0)
+                                       | (16 if factor == "chol_lu" else 0) | (4 if texp else 0)
                                        | (8 if reverse_sums else 0)),
            "rbf_interpolation")
     return gout, its.value, reason.value

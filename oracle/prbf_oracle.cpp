@@ -402,6 +402,61 @@ void gpu_tri_apply(int nb, int b0, const double* Lp, double* y) {
   }
 }
 
+// The GPU library's LU fallback for a block whose ordered Cholesky meets a non-positive
+// pivot (PETSc's -sub_pc_type lu semantics on its blocks, restated in its arithmetic): K
+// mirrored to a full matrix, then LU with partial pivoting -- pivot the first row of
+// largest |a_ik|, full rows swapped, l_ik = a_ik / a_kk, a_ij = fma(-l_ik, a_kj, a_ij).
+// Returns false on an exactly zero pivot (where PETSc's LU stops).
+bool gpu_lu_factor(int n, double* A, int* piv) {
+  for (int i = 0; i < n; i++)
+    for (int j = i + 1; j < n; j++) A[(size_t)i * n + j] = A[(size_t)j * n + i];
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    double amax = fabs(A[(size_t)k * n + k]);
+    for (int i = k + 1; i < n; i++) {
+      const double v = fabs(A[(size_t)i * n + k]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    piv[k] = p;
+    if (amax == 0.0) return false;
+    if (p != k)
+      for (int j = 0; j < n; j++) std::swap(A[(size_t)k * n + j], A[(size_t)p * n + j]);
+    const double d = A[(size_t)k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      double* ri = A + (size_t)i * n;
+      const double l = ri[k] / d;
+      ri[k] = l;
+      const double* rk = A + (size_t)k * n;
+      for (int j = k + 1; j < n; j++) ri[j] = std::fma(-l, rk[j], ri[j]);
+    }
+  }
+  return true;
+}
+
+// Its solve, y <- scale * K^-1 y in the GPU's per-entry order: the row interchanges in
+// order, forward (unit lower) with fma over ascending columns, backward with fma over
+// descending columns and a division by the pivot, then the scale (2 pi sigma^2).
+void gpu_lu_solve(int n, const double* A, const int* piv, double scale, double* y) {
+  for (int k = 0; k < n; k++)
+    if (piv[k] != k) std::swap(y[k], y[piv[k]]);
+  for (int i = 0; i < n; i++) {
+    const double* ri = A + (size_t)i * n;
+    double v = y[i];
+    for (int j = 0; j < i; j++) v = std::fma(-ri[j], y[j], v);
+    y[i] = v;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    const double* ri = A + (size_t)i * n;
+    double v = y[i];
+    for (int j = n - 1; j > i; j--) v = std::fma(-ri[j], y[j], v);
+    y[i] = v / ri[i];
+  }
+  for (int i = 0; i < n; i++) y[i] = y[i] * scale;
+}
+
 // Deterministic sum: fixed 256 chunks summed in order, independent of thread count.
 double det_dot(int n, const double* a, const double* b) {
   const int nch = 256;
@@ -428,10 +483,17 @@ struct Rasm {
   std::vector<double> lu;             // LU factors (row-major)
   std::vector<int> piv;               // pivot rows, per block (offset = off)
   int basic = 0;                      // PETSc -pc_asm_type basic instead of restrict
-  int kind = 0;                       // 0: dense LU (the reference's); 1: the GPU's Cholesky
+  int kind = 0;                       // 0: dense LU (the reference's); 1: the GPU's Cholesky;
+                                      // 2: the GPU's Cholesky with its LU fallback
+  double sigma = 0.0;
   std::vector<long long> coff;        // kind 1: packed-factor offsets (nb (nb + 1) / 2 each)
   std::vector<double> chol;           // kind 1: packed factors (gpu_chol_pack)
   int nshifted = 0;                   // kind 1: blocks refactored with a diagonal shift
+                                      // (kind 2: blocks refactored by LU)
+  std::vector<long long> luoff;       // kind 2: per cell, offset of its LU factor or -1
+  std::vector<double> lub;            // kind 2: LU factors of those blocks (nb x nb each)
+  std::vector<int> lupiv;             // kind 2: their pivot rows (nb each, at luoff / nb)
+  std::vector<long long> lupoff;      // kind 2: per cell, offset of its pivots
 };
 
 // Dense LU with partial pivoting (row interchanges), the algorithm PETSc's
@@ -646,7 +708,7 @@ void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y
 // ordered Cholesky with the GPU's shifted retries (diagonal + 1e-12, then + 1e-9, relative
 // to K's unit diagonal) for blocks with a non-positive pivot, packed factors.
 static int rasm_build_chol(const orc_grid* g, Rasm* R, const std::vector<int>& cnt, const double* x,
-                           const double* y, const double* z) {
+                           const double* y, const double* z, bool lu_fallback) {
   R->coff.assign(g->ncell + 1, 0);
   for (int c = 0; c < g->ncell; c++)
     R->coff[c + 1] = R->coff[c] + (long long)cnt[c] * (cnt[c] + 1) / 2;
@@ -655,6 +717,7 @@ static int rasm_build_chol(const orc_grid* g, Rasm* R, const std::vector<int>& c
   const double out_scale = 2.0 * M_PI * g->sigma * g->sigma;
   const double sc = sqrt(1.0 / out_scale);
   int bad = 0, shifted = 0;
+  std::vector<unsigned char> need_lu(g->ncell, 0);
 #pragma omp parallel reduction(| : bad) reduction(+ : shifted)
   {
     std::vector<double> K, U;
@@ -670,19 +733,50 @@ static int rasm_build_chol(const orc_grid* g, Rasm* R, const std::vector<int>& c
         const double shift = attempt == 0 ? 0.0 : (attempt == 1 ? 1e-12 : 1e-9);
         gpu_block_K(g->dim, nb, nc, R->idx.data() + R->off[c], x, y, z, kexp, shift, K.data());
         ok = gpu_chol_pack(nb, K.data(), sc, U.data(), R->chol.data() + R->coff[c]);
-        if (!ok && attempt == 0) shifted++;
+        if (!ok && attempt == 0) {
+          shifted++;
+          if (lu_fallback) {
+            need_lu[c] = 1;
+            ok = true;  // factored below
+          }
+        }
       }
       if (!ok) bad = 1;
     }
   }
   R->nshifted = shifted;
+  if (lu_fallback) {
+    // the LU fallback (kind 2), blocks in cell order
+    R->luoff.assign(g->ncell, -1);
+    R->lupoff.assign(g->ncell, -1);
+    long long a = 0, p = 0;
+    for (int c = 0; c < g->ncell; c++)
+      if (need_lu[c]) {
+        R->luoff[c] = a;
+        R->lupoff[c] = p;
+        a += (long long)cnt[c] * cnt[c];
+        p += cnt[c];
+      }
+    R->lub.assign(a, 0.0);
+    R->lupiv.assign(p, 0);
+    for (int c = 0; c < g->ncell; c++) {
+      if (!need_lu[c]) continue;
+      const int nb = cnt[c], nc = R->cs[c + 1] - R->cs[c];
+      double* K = R->lub.data() + R->luoff[c];
+      gpu_block_K(g->dim, nb, nc, R->idx.data() + R->off[c], x, y, z, kexp, 0.0, K);
+      if (!gpu_lu_factor(nb, K, R->lupiv.data() + R->lupoff[c])) bad = 1;
+    }
+  }
   return bad ? ERR_SINGULAR : OK;
 }
+
+static bool lu_block(const Rasm* R, int c) { return R->kind == 2 && R->luoff[c] >= 0; }
 
 void* orc_rasm_create_kind(const orc_grid* g, int n, const double* x, const double* y,
                            const double* z, const int* cs, int kind, int* status) {
   Rasm* R = new Rasm;
-  R->kind = kind == 1 ? 1 : 0;
+  R->kind = (kind == 1 || kind == 2) ? kind : 0;
+  R->sigma = g->sigma;
   R->n = n;
   R->ncell = g->ncell;
   R->cs.assign(cs, cs + g->ncell + 1);
@@ -698,8 +792,8 @@ void* orc_rasm_create_kind(const orc_grid* g, int n, const double* x, const doub
   }
   R->idx.resize(R->off[g->ncell]);
   orc_buffer_fill(g, x, y, z, cs, R->off.data(), R->idx.data());
-  if (R->kind == 1) {
-    int st = rasm_build_chol(g, R, cnt, x, y, z);
+  if (R->kind >= 1) {
+    int st = rasm_build_chol(g, R, cnt, x, y, z, R->kind == 2);
     if (status) *status = st;
     return R;
   }
@@ -736,11 +830,15 @@ static void asm_basic_apply(const Rasm* R, const double* r, double* out) {
     if (!nb) continue;
     double* buf = sol.data() + R->off[c];
     const int* id = R->idx.data() + R->off[c];
-    if (R->kind == 1) {
+    if (R->kind >= 1) {
       const int nc = R->cs[c + 1] - R->cs[c];
       std::vector<double> yb(nb);
       for (long long j = 0; j < nb; j++) yb[j] = r[id[gpu_row((int)j, (int)nb, nc)]];
-      gpu_tri_apply((int)nb, 0, R->chol.data() + R->coff[c], yb.data());
+      if (lu_block(R, c))
+        gpu_lu_solve((int)nb, R->lub.data() + R->luoff[c], R->lupiv.data() + R->lupoff[c],
+                     2.0 * M_PI * R->sigma * R->sigma, yb.data());
+      else
+        gpu_tri_apply((int)nb, 0, R->chol.data() + R->coff[c], yb.data());
       for (long long j = 0; j < nb; j++) buf[gpu_row((int)j, (int)nb, nc)] = yb[j];
       continue;
     }
@@ -769,10 +867,14 @@ int orc_rasm_apply(void* h, const double* r, double* out) {
       buf.resize(nb);
       const int* id = R->idx.data() + R->off[c];
       int nc = R->cs[c + 1] - R->cs[c];
-      if (R->kind == 1) {
+      if (R->kind >= 1) {
         const int n1 = (int)nb - nc;
         for (long long j = 0; j < nb; j++) buf[j] = r[id[gpu_row((int)j, (int)nb, nc)]];
-        gpu_tri_apply((int)nb, n1, R->chol.data() + R->coff[c], buf.data());
+        if (lu_block(R, c))
+          gpu_lu_solve((int)nb, R->lub.data() + R->luoff[c], R->lupiv.data() + R->lupoff[c],
+                       2.0 * M_PI * R->sigma * R->sigma, buf.data());
+        else
+          gpu_tri_apply((int)nb, n1, R->chol.data() + R->coff[c], buf.data());
         for (int i = 0; i < nc; i++) out[R->cs[c] + i] = buf[n1 + i];
         continue;
       }
@@ -797,7 +899,7 @@ int orc_rasm_block_info(void* h, int cell, int* nb, int* nc, int* nshifted) {
 
 int orc_rasm_factor_rows(void* h, int cell, double* out) {
   Rasm* R = (Rasm*)h;
-  if (!R || R->kind != 1 || cell < 0 || cell >= R->ncell) return ERR_ARG;
+  if (!R || R->kind < 1 || cell < 0 || cell >= R->ncell || lu_block(R, cell)) return ERR_ARG;
   std::copy(R->chol.begin() + R->coff[cell], R->chol.begin() + R->coff[cell + 1], out);
   return OK;
 }
@@ -984,7 +1086,8 @@ int orc_rbf_interpolation(int dim, int n, const double* x, const double* y, cons
     fs[k] = f[perm[k]];
   }
   const double* zp = dim == 3 ? zs.data() : nullptr;
-  void* R = orc_rasm_create_kind(&g, n, xs.data(), ys.data(), zp, cs.data(), (pc_flags & 2) ? 1 : 0, &st);
+  void* R = orc_rasm_create_kind(&g, n, xs.data(), ys.data(), zp, cs.data(),
+                                 (pc_flags & 2) ? ((pc_flags & 16) ? 2 : 1) : 0, &st);
   if (st) {
     orc_rasm_destroy(R);
     return st;

@@ -64,7 +64,9 @@ void* orc_rasm_create(const orc_grid* g, int n, const double* x, const double* y
                       const double* z, const int* cs, int* status);
 /* kind 0: dense LU with partial pivoting (PETSc's -sub_pc_type lu, the reference's);
  * kind 1: the GPU library's arithmetic -- blocks K = 2 pi sigma^2 A_c with the neighbour
- * points first, its table exp, the ordered Cholesky and the apply's substitution order. */
+ * points first, its table exp, the ordered Cholesky and the apply's substitution order;
+ * kind 2: kind 1 with the GPU's LU fallback (a block whose Cholesky meets a non-positive
+ * pivot is factored by LU with partial pivoting instead of shifted; a zero pivot fails). */
 void* orc_rasm_create_kind(const orc_grid* g, int n, const double* x, const double* y,
                            const double* z, const int* cs, int kind, int* status);
 int orc_rasm_block_info(void* h, int cell, int* nb, int* nc, int* nshifted);
@@ -92,7 +94,8 @@ int orc_gmres_ex(const orc_grid* g, int n, const double* x, const double* y,
 
 /* pc_flags: bit 0 basic additive Schwarz (-pc_asm_type basic); bit 1 the GPU's Cholesky
  * blocks (kind 1) instead of LU; bit 2 the GPU's table exp in the Gaussian sums; bit 3 the
- * sums' terms added in reverse order (a rounding-order probe). */
+ * sums' terms added in reverse order (a rounding-order probe); bit 4 with bit 1, the LU
+ * fallback (kind 2). */
 int orc_rbf_interpolation(int dim, int n, const double* x, const double* y,
                           const double* z, const double* f, double sigma,
                           int nsigma_box, int sigma_buffer, int sigma_trunc,

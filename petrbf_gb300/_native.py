@@ -19,7 +19,8 @@ class Params(ctypes.Structure):
                 ("sigma_buffer", ctypes.c_int), ("sigma_trunc", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("abstol", ctypes.c_double), ("dtol", ctypes.c_double),
                 ("restart", ctypes.c_int), ("max_it", ctypes.c_int), ("precision", ctypes.c_int),
-                ("guess", ctypes.c_int), ("device", ctypes.c_int), ("pc_type", ctypes.c_int)]
+                ("guess", ctypes.c_int), ("device", ctypes.c_int), ("pc_type", ctypes.c_int),
+                ("block_fallback", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -64,6 +65,7 @@ OK, ERR_ARG, ERR_RANGE, ERR_CAPACITY, ERR_CUDA, ERR_NOT_CONVERGED, ERR_BREAKDOWN
 PREC_FP64, PREC_MIXED = 0, 1
 GUESS_ZERO, GUESS_LEARNED = 0, 1
 PC_RASM, PC_ASM = 0, 1
+FALLBACK_SHIFT, FALLBACK_LU = 0, 1
 ORDER_CALLER, ORDER_CELL, MATVEC_FP32 = 0, 1, 2
 
 # Every function the header declares, with its ctypes signature.

@@ -35,7 +35,7 @@ class Context:
 
     def __init__(self, dim=2, sigma=0.025, nsigma_box=8, sigma_buffer=24, sigma_trunc=24,
                  rtol=1e-13, abstol=1e-50, dtol=1e5, restart=30, max_it=1000, precision="fp64",
-                 guess="zero", device=0, pc="rasm"):
+                 guess="zero", device=0, pc="rasm", block_fallback="shift"):
         L = N.lib()
         p = N.Params()
         L.prbf_params_default(ctypes.byref(p))
@@ -46,6 +46,9 @@ class Context:
         p.precision = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
         p.guess = {"zero": N.GUESS_ZERO, "learned": N.GUESS_LEARNED}[guess]
         p.pc_type = {"rasm": N.PC_RASM, "asm": N.PC_ASM}[pc]
+        # "lu": a block whose FP64 Cholesky fails is factored by LU with partial pivoting, as
+        # the reference's PETSc LU (a zero pivot raises); "shift": refactored with a shift
+        p.block_fallback = {"shift": N.FALLBACK_SHIFT, "lu": N.FALLBACK_LU}[block_fallback]
         self.params = p
         self.dim = p.dim
         h = ctypes.c_void_p()

@@ -346,6 +346,7 @@ void batch_interpolate(Ctx& c, int nprob, const prbf_problem* probs, int* its_ou
   G.cell_sigma = B.csig.get();
   size_t free_b = 0, total_b = 0;
   PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  B.rasm.lu_fallback = p.block_fallback == PRBF_FALLBACK_LU;
   rasm_factor(B.rasm, G, hcnt_all, B.hcs, mixed, c.ws, c.err.get(), c.stream, std::min(16.0e9, 0.25 * (double)free_b),
               true, p.pc_type == PRBF_PC_ASM);
   rasm_set_apply_smem(B.rasm);

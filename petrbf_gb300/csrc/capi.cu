@@ -149,6 +149,7 @@ void prbf_params_default(prbf_params* p) {
   p->guess = PRBF_GUESS_ZERO;
   p->device = 0;
   p->pc_type = PRBF_PC_RASM;
+  p->block_fallback = PRBF_FALLBACK_SHIFT;
 }
 
 const char* prbf_status_string(int s) {
@@ -175,6 +176,7 @@ int prbf_ctx_create(const prbf_params* p, prbf_ctx** out) {
   if (p->dim != 2 && p->dim != 3) return PRBF_ERR_ARG;
   if (!(p->sigma > 0) || p->nsigma_box <= 0 || p->restart <= 0 || p->max_it < 0) return PRBF_ERR_ARG;
   if (p->pc_type != PRBF_PC_RASM && p->pc_type != PRBF_PC_ASM) return PRBF_ERR_ARG;
+  if (p->block_fallback != PRBF_FALLBACK_SHIFT && p->block_fallback != PRBF_FALLBACK_LU) return PRBF_ERR_ARG;
   prbf_ctx* ctx = new (std::nothrow) prbf_ctx();
   if (!ctx) return PRBF_ERR_CAPACITY;
   ctx->c.p = *p;

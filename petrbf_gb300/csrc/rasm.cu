@@ -1114,9 +1114,11 @@ __global__ void __launch_bounds__(256) k_apply_tri(int ncell, const long long* _
                                                    const long long* __restrict__ loff, const T* __restrict__ Lpack,
                                                    const double* __restrict__ r, double* __restrict__ out,
                                                    long long vs, const int* __restrict__ skip, int full,
-                                                   double* __restrict__ Y, long long ys, SegSkip seg) {
+                                                   double* __restrict__ Y, long long ys, SegSkip seg,
+                                                   const int* __restrict__ lu_of_cell) {
   if (skip && *skip) return;
   if (seg.cell_done(blockIdx.x)) return;
+  if (lu_of_cell && lu_of_cell[blockIdx.x] >= 0) return;  // factored by LU: k_apply_lu
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tri[32][33];
   const int c = blockIdx.x;
@@ -1464,6 +1466,157 @@ __global__ void __launch_bounds__(kTrwWarps * 32) k_apply_trw(int ncell, const l
   }
 }
 
+// ---- LU fallback of the FP64 form (one CTA per block, in global memory) -------------
+// For the few blocks whose ordered Cholesky meets a non-positive pivot: K (lower triangle
+// as assembled) mirrored to a full matrix, then LU with partial pivoting -- pivot the first
+// row of largest |a_ik| (a tree reduction that keeps the smaller row on ties), full rows
+// swapped, l_ik = a_ik / a_kk, a_ij = fma(-l_ik, a_kj, a_ij) -- the entry-wise operations of
+// the unblocked loop, so a CPU restatement of that loop reproduces the factor bit for bit.
+// bad[b] = 1 on an exactly zero pivot (where PETSc's LU stops).
+constexpr int kLuThreads = 256;
+
+__global__ void __launch_bounds__(kLuThreads) k_lu_fp64(int nlu, const int* __restrict__ lucell,
+                                                        const long long* __restrict__ boff,
+                                                        const long long* __restrict__ koff, double* __restrict__ LU,
+                                                        const long long* __restrict__ poff, int* __restrict__ piv,
+                                                        unsigned char* __restrict__ bad) {
+  const int b = blockIdx.x;
+  if (b >= nlu) return;
+  const int c = lucell[b];
+  const int n = (int)(boff[c + 1] - boff[c]);
+  double* A = LU + koff[b];
+  int* pv = piv + poff[b];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  constexpr int NW = kLuThreads / 32;
+  __shared__ double s_v[kLuThreads];
+  __shared__ int s_i[kLuThreads];
+  __shared__ int s_bad;
+  for (int i = w; i < n; i += NW)
+    for (int j = i + 1 + lane; j < n; j += 32) A[(long long)i * n + j] = A[(long long)j * n + i];
+  if (tid == 0) s_bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; k++) {
+    double bv = -1.0;
+    int bi = n;
+    for (int i = k + tid; i < n; i += kLuThreads) {
+      const double v = fabs(A[(long long)i * n + k]);
+      if (v > bv) {
+        bv = v;
+        bi = i;
+      }
+    }
+    s_v[tid] = bv;
+    s_i[tid] = bi;
+    __syncthreads();
+    for (int st = kLuThreads / 2; st > 0; st >>= 1) {
+      if (tid < st) {
+        const double ov = s_v[tid + st];
+        const int oi = s_i[tid + st];
+        if (ov > s_v[tid] || (ov == s_v[tid] && oi < s_i[tid])) {
+          s_v[tid] = ov;
+          s_i[tid] = oi;
+        }
+      }
+      __syncthreads();
+    }
+    const int p = s_i[0];
+    const bool zero = p >= n || s_v[0] == 0.0;
+    if (tid == 0) {
+      pv[k] = zero ? k : p;
+      if (zero) s_bad = 1;
+    }
+    if (zero) break;  // uniform over the CTA
+    if (p != k)
+      for (int j = tid; j < n; j += kLuThreads) {
+        const double t = A[(long long)k * n + j];
+        A[(long long)k * n + j] = A[(long long)p * n + j];
+        A[(long long)p * n + j] = t;
+      }
+    __syncthreads();
+    const double d = A[(long long)k * n + k];
+    for (int i = k + 1 + tid; i < n; i += kLuThreads) A[(long long)i * n + k] = __ddiv_rn(A[(long long)i * n + k], d);
+    __syncthreads();
+    for (int i = k + 1 + w; i < n; i += NW) {
+      const double l = A[(long long)i * n + k];
+      for (int j = k + 1 + lane; j < n; j += 32)
+        A[(long long)i * n + j] = __fma_rn(-l, A[(long long)k * n + j], A[(long long)i * n + j]);
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (tid == 0) bad[b] = (unsigned char)s_bad;
+}
+
+// The LU blocks' share of an apply: y <- 2 pi sigma^2 K^-1 y in the entry-wise order of the
+// sequential solve (interchanges in order; forward, y_i receiving fma(-l_ik, y_k, .) for
+// ascending k; backward, descending k with the division by the pivot when y_k is final),
+// then the restricted (centre rows) or basic (all slots) output of k_apply_tri.
+__global__ void __launch_bounds__(kLuThreads) k_apply_lu(int nlu, const int* __restrict__ lucell,
+                                                         const long long* __restrict__ boff,
+                                                         const int* __restrict__ cs, const int* __restrict__ idx,
+                                                         const long long* __restrict__ koff,
+                                                         const double* __restrict__ LU,
+                                                         const long long* __restrict__ poff,
+                                                         const int* __restrict__ piv, const double* __restrict__ r,
+                                                         double* __restrict__ out, long long vs, int nv,
+                                                         const int* __restrict__ skip, int full,
+                                                         double* __restrict__ Y, long long ys, SegSkip seg,
+                                                         double scale_all, const double* __restrict__ cell_sig) {
+  if (skip && *skip) return;
+  const int b = blockIdx.x;
+  if (b >= nlu) return;
+  const int c = lucell[b];
+  if (seg.cell_done(c)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nb = (int)(boff[c + 1] - boff[c]);
+  const int nc = cs[c + 1] - cs[c], n1 = nb - nc;
+  const int* id = idx + boff[c];
+  const double* A = LU + koff[b];
+  const int* pv = piv + poff[b];
+  double* y = (double*)smem_raw;  // nv x nb
+  const int tid = threadIdx.x;
+  for (int j = tid; j < nb; j += kLuThreads) {
+    const int p = id[j < n1 ? nc + j : j - n1];
+    for (int v = 0; v < nv; v++) y[v * nb + j] = r[v * vs + p];
+  }
+  __syncthreads();
+  if (tid < nv)
+    for (int k = 0; k < nb; k++) {
+      const int p = pv[k];
+      if (p != k) {
+        const double t = y[tid * nb + k];
+        y[tid * nb + k] = y[tid * nb + p];
+        y[tid * nb + p] = t;
+      }
+    }
+  __syncthreads();
+  for (int k = 0; k < nb; k++) {
+    for (int i = k + 1 + tid; i < nb; i += kLuThreads) {
+      const double l = A[(long long)i * nb + k];
+      for (int v = 0; v < nv; v++) y[v * nb + i] = __fma_rn(-l, y[v * nb + k], y[v * nb + i]);
+    }
+    __syncthreads();
+  }
+  for (int k = nb - 1; k >= 0; k--) {
+    if (tid < nv) y[tid * nb + k] = __ddiv_rn(y[tid * nb + k], A[(long long)k * nb + k]);
+    __syncthreads();
+    for (int i = tid; i < k; i += kLuThreads) {
+      const double u = A[(long long)i * nb + k];
+      for (int v = 0; v < nv; v++) y[v * nb + i] = __fma_rn(-u, y[v * nb + k], y[v * nb + i]);
+    }
+    __syncthreads();
+  }
+  const double scale = cell_sig ? 2.0 * M_PI * cell_sig[c] * cell_sig[c] : scale_all;
+  if (full) {
+    double* Yc = Y + boff[c];
+    for (int j = tid; j < nb; j += kLuThreads)
+      for (int v = 0; v < nv; v++) Yc[v * ys + (j < n1 ? nc + j : j - n1)] = __dmul_rn(y[v * nb + j], scale);
+  } else {
+    for (int i = tid; i < nc; i += kLuThreads)
+      for (int v = 0; v < nv; v++) out[v * vs + cs[c] + i] = __dmul_rn(y[v * nb + n1 + i], scale);
+  }
+}
+
 // basic Schwarz: out[i] = sum of the slots of point i (ascending slot = ascending block)
 __global__ void k_asm_gather(int n, int nv, const long long* __restrict__ inv_off,
                              const long long* __restrict__ inv_slot, const double* __restrict__ Y, long long ys,
@@ -1564,6 +1717,8 @@ void rasm_block_K(const RasmPlan& R, const PointSet& P, int cell, int nb, double
 }
 
 void rasm_factor_rows(const RasmPlan& R, int cell, int nb, double* out, cudaStream_t s) {
+  if (std::binary_search(R.lu_cells.begin(), R.lu_cells.end(), cell))
+    throw Error(PRBF_ERR_STATE, "the block of this cell was factored by LU (no Cholesky factor)");
   if (!R.factor || R.fp32) throw Error(PRBF_ERR_STATE, "the plan keeps no FP64 factor");
   long long lo[2];
   PRBF_CUDA(cudaMemcpyAsync(lo, R.loff.get() + cell, sizeof(lo), cudaMemcpyDeviceToHost, s));
@@ -1582,6 +1737,56 @@ void rasm_buffer_lists(const PointSet& P, int* counts_dev, const long long* boff
                                                       boff_dev ? 1 : 0, counts_dev, boff_dev, idx_dev);
   PRBF_CHECK_LAUNCH();
 }
+
+namespace {
+// The LU fallback's blocks (cells, any order): K assembled unshifted into their own
+// storage, factored by k_lu_fp64; a zero pivot is the reference's PETSc LU failure.
+void lu_build(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, std::vector<int> cells, Workspace& ws,
+              cudaStream_t s) {
+  std::sort(cells.begin(), cells.end());
+  const int nlu = (int)cells.size();
+  std::vector<long long> hk(nlu + 1, 0), hp(nlu + 1, 0);
+  std::vector<int> hmap(G.ncell, -1);
+  for (int b = 0; b < nlu; b++) {
+    const long long nb = hcnt[cells[b]];
+    hk[b + 1] = hk[b] + nb * nb;
+    hp[b + 1] = hp[b] + nb;
+    hmap[cells[b]] = b;
+  }
+  R.lucell.reserve(nlu);
+  R.lukoff.reserve(nlu + 1);
+  R.lupoff.reserve(nlu + 1);
+  R.lu_of_cell.reserve(G.ncell);
+  R.LU64.reserve(std::max<long long>(hk[nlu], 1));
+  R.lupiv.reserve(std::max<long long>(hp[nlu], 1));
+  PRBF_CUDA(cudaMemcpyAsync(R.lucell.get(), cells.data(), sizeof(int) * nlu, cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyAsync(R.lukoff.get(), hk.data(), sizeof(long long) * (nlu + 1), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyAsync(R.lupoff.get(), hp.data(), sizeof(long long) * (nlu + 1), cudaMemcpyHostToDevice, s));
+  PRBF_CUDA(cudaMemcpyAsync(R.lu_of_cell.get(), hmap.data(), sizeof(int) * G.ncell, cudaMemcpyHostToDevice, s));
+  const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
+  for (int b0 = 0; b0 < nlu; b0 += 65535) {  // gridDim.y of the assembly
+    const int m = std::min(65535, nlu - b0);
+    k_assemble<double><<<dim3(64, m), 256, 0, s>>>(m, R.lucell.get() + b0, R.boff.get(), G.cs, R.idx.get(),
+                                                   R.lukoff.get() + b0, G.x, G.y, G.z, G.dim, inv2s2, G.cell_sigma,
+                                                   0.0, R.LU64.get(), nullptr, nullptr, 0, kexp_of_sigma(G.sigma),
+                                                   exp_table_dev(s));
+    PRBF_CHECK_LAUNCH();
+  }
+  unsigned char* dbad = (unsigned char*)ws.get(50, nlu);
+  k_lu_fp64<<<nlu, kLuThreads, 0, s>>>(nlu, R.lucell.get(), R.boff.get(), R.lukoff.get(), R.LU64.get(),
+                                        R.lupoff.get(), R.lupiv.get(), dbad);
+  PRBF_CHECK_LAUNCH();
+  std::vector<unsigned char> hbad(nlu);
+  PRBF_CUDA(cudaMemcpyAsync(hbad.data(), dbad, nlu, cudaMemcpyDeviceToHost, s));
+  PRBF_CUDA(cudaStreamSynchronize(s));
+  for (int b = 0; b < nlu; b++)
+    if (hbad[b])
+      throw Error(PRBF_ERR_FACTOR, "zero pivot in the LU of a subdomain block (duplicated points): the reference's "
+                                   "PETSc LU stops here as well");
+  R.nlu = nlu;
+  R.lu_cells = cells;
+}
+}  // namespace
 
 void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, const std::vector<int>& hcs, bool fp32,
                  Workspace& ws, unsigned* err, cudaStream_t s, double ws_budget_bytes, bool factor, bool basic) {
@@ -1662,6 +1867,11 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   R.nfallback = 0;
   R.retried.clear();
+  R.nlu = 0;
+  R.lu_cells.clear();
+  R.lu_scale = 2.0 * M_PI * G.sigma * G.sigma;
+  R.lu_cell_sigma = G.cell_sigma;
+  std::vector<int> lu_cells;
   // FP32 form: the coordinates split into float pairs once (the assembly then stays on the
   // FP32 pipes)
   float2* hl = nullptr;
@@ -1746,11 +1956,18 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
         if (hbad[k] && attempt == 0) R.retried.push_back(bc[k]);
       }
       if (nbad == 0) break;
+      if (!fp32 && R.lu_fallback) {  // factored by LU after the batches, unshifted
+        for (int k = 0; k < nb_batch; k++)
+          if (hbad[k]) lu_cells.push_back(bc[k]);
+        R.nfallback += nbad;
+        break;
+      }
       if (attempt == 2) throw Error(PRBF_ERR_FACTOR, "subdomain block not positive definite after shifted retries");
       R.nfallback += nbad;
     }
     pos = q;
   }
+  if (!lu_cells.empty()) lu_build(R, G, hcnt, lu_cells, ws, s);
 }
 
 namespace {
@@ -1784,22 +2001,23 @@ void apply_tri_nv(const RasmPlan& R, const T* Lp, const int* cs, const double* r
     }
   } else {
     const size_t sm = (size_t)nv * R.max_nb * sizeof(T);
+    const int* luc = R.nlu ? R.lu_of_cell.get() : nullptr;
     switch (nv) {
       case 1:
         k_apply_tri<T, 1><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
-                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg, luc);
         break;
       case 2:
         k_apply_tri<T, 2><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
-                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg, luc);
         break;
       case 3:
         k_apply_tri<T, 3><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
-                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg, luc);
         break;
       default:
         k_apply_tri<T, 4><<<R.ncell, 256, sm, s>>>(R.ncell, R.boff.get(), cs, R.idx.get(), R.loff.get(), Lp, r, out,
-                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg);
+                                                   vs, skip, full, R.Y.get(), R.nslot, R.seg, luc);
         break;
     }
   }
@@ -1837,10 +2055,18 @@ void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, 
     const double* rv = r + v0 * vstride;
     double* ov = out + v0 * vstride;
     if (R.factor) {
-      if (R.fp32)
+      if (R.fp32) {
         apply_tri_nv<float>(R, R.L32.get(), cs, rv, ov, vstride, k, s, skip);
-      else
+      } else {
         apply_tri_nv<double>(R, R.L64.get(), cs, rv, ov, vstride, k, s, skip);
+        if (R.nlu) {
+          k_apply_lu<<<R.nlu, kLuThreads, (size_t)k * R.max_nb * sizeof(double), s>>>(
+              R.nlu, R.lucell.get(), R.boff.get(), cs, R.idx.get(), R.lukoff.get(), R.LU64.get(), R.lupoff.get(),
+              R.lupiv.get(), rv, ov, vstride, k, skip, R.basic ? 1 : 0, R.Y.get(), R.nslot, R.seg, R.lu_scale,
+              R.lu_cell_sigma);
+          PRBF_CHECK_LAUNCH();
+        }
+      }
     } else {
       for (int v = 0; v < k; v++) {
         const size_t sm = (size_t)R.max_nb * sizeof(float);
@@ -1858,6 +2084,11 @@ void rasm_apply(const RasmPlan& R, const int* cs, const double* r, double* out, 
 }
 
 void rasm_set_apply_smem(const RasmPlan& R) {
+  if (R.nlu) {
+    const size_t sm = (size_t)std::max(1, std::min(4, R.max_nv)) * std::max(R.max_nb, 1) * sizeof(double);
+    if (sm > 220 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the LU apply's shared memory");
+    PRBF_CUDA(cudaFuncSetAttribute(k_apply_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  }
   if (R.factor) {
     if (R.fp32)
       set_tri_smem<float>(R);

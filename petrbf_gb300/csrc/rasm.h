@@ -28,6 +28,19 @@ struct RasmPlan {
   SegSkip seg;                // batches: skip the blocks of stopped problems (when seg.done set)
   int max_nv = 1;             // right-hand sides per apply launch (1..4; set before the build)
   long long nslot = 0;        // basic form: buffer-list entries (slot stride of Y)
+  // FP64 form, set before the build: a block whose Cholesky meets a non-positive pivot is
+  // factored by LU with partial pivoting (the reference's PETSc LU) instead of shifted
+  bool lu_fallback = false;
+  int nlu = 0;                     // blocks factored by LU
+  std::vector<int> lu_cells;       // their cells, ascending (host)
+  DevBuf<int> lucell;              // their cells (device)
+  DevBuf<long long> lukoff;        // per LU block: offset of its nb x nb factor in LU64
+  DevBuf<long long> lupoff;        // per LU block: offset of its nb pivot rows in lupiv
+  DevBuf<int> lu_of_cell;          // per cell: its LU block, or -1 (ncell)
+  DevBuf<double> LU64;             // the LU factors (row-major, unit lower L below U)
+  DevBuf<int> lupiv;               // their pivot rows
+  double lu_scale = 0.0;           // 2 pi sigma^2 (A^-1 = 2 pi sigma^2 K^-1)
+  const double* lu_cell_sigma = nullptr;  // batches: per-cell sigma (device), else null
 };
 
 // Buffer lists, blocks, factorisations and S_c for every non-empty cell of P.
@@ -60,7 +73,8 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
 void rasm_block_K(const RasmPlan& R, const PointSet& P, int cell, int nb, double* K_dev, Workspace& ws,
                   cudaStream_t s);
 // The FP64 factor of one block as stored (row i: L_A[i][0..i-1] then 1/L_A[i][i]), the
-// rows' padding removed, into out (host, nb (nb + 1) / 2 entries).
+// rows' padding removed, into out (host, nb (nb + 1) / 2 entries). PRBF_ERR_STATE for a
+// block factored by LU.
 void rasm_factor_rows(const RasmPlan& R, int cell, int nb, double* out, cudaStream_t s);
 // Sets the dynamic shared memory limit of the apply kernel for this plan.
 void rasm_set_apply_smem(const RasmPlan& R);

@@ -108,6 +108,7 @@ static void interpolate(Ctx& c, int n, const double* x, const double* y, const d
   // FP32 blocks: S_c (one GEMV per apply) in 2D; in 3D the blocks are too ill-conditioned
   // for an explicit FP32 inverse, so the FP32 factor is kept and applied by substitution
   S.rasm.max_nv = std::min(4, nrhs);
+  S.rasm.lu_fallback = p.block_fallback == PRBF_FALLBACK_LU;
   rasm_build(S.rasm, S.pts, mixed, c.ws, c.err.get(), c.stream, budget, mixed && dim == 3,
              p.pc_type == PRBF_PC_ASM);
   rasm_set_apply_smem(S.rasm);
@@ -372,6 +373,7 @@ int prbf_pc_setup(prbf_ctx* ctx, int precision) {
     size_t free_b = 0, total_b = 0;
     PRBF_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const bool fp32 = precision == PRBF_PREC_MIXED;
+    c.solve->pc.lu_fallback = c.p.block_fallback == PRBF_FALLBACK_LU;
     rasm_build(c.solve->pc, c.mv_pts, fp32, c.ws, c.err.get(), c.stream, std::min(16.0e9, 0.25 * (double)free_b),
                fp32 && c.mv_pts.g.dim == 3, c.p.pc_type == PRBF_PC_ASM);
     rasm_set_apply_smem(c.solve->pc);

@@ -8,12 +8,18 @@ the C ABI (prbf_pc_buffer_lists, prbf_pc_block, prbf_pc_apply):
   library's block arithmetic;
 * the FP64 factors and the preconditioner applies are bit-identical to that restatement
   (oracle Rasm factor="chol"), so one point moved between subdomains, or one operation
-  reordered, fails these tests."""
+  reordered, fails these tests;
+* with block_fallback="lu" the blocks whose Cholesky fails are factored by LU with partial
+  pivoting (the reference's -sub_pc_type lu on them): the applies are bit-identical to the
+  oracle's restatement of that fallback (factor="chol_lu"), and an exactly singular block
+  (duplicated points) is the reference's zero-pivot failure."""
 import numpy as np
 import pytest
 
 import oracle as O
-from petrbf_gb300.api import Context
+from petrbf_gb300 import _native as N
+from petrbf_gb300 import workloads as W
+from petrbf_gb300.api import Context, PrbfError
 
 pytestmark = pytest.mark.gpu
 
@@ -134,3 +140,62 @@ def test_fp64_apply_equals_oracle_restatement(golden, case, pc):
     lu = np.empty(n)
     lu[perm] = L.apply(r[perm])
     assert np.linalg.norm(out - lu) / np.linalg.norm(lu) < 1e-7
+
+
+@pytest.mark.parametrize("case", ["g2d_ragged", "g2d_jitter48"])
+@pytest.mark.parametrize("pc", ["rasm", "asm"])
+def test_lu_fallback_apply_equals_oracle_restatement(golden, case, pc):
+    d = golden(case)
+    g, xs, ys, zs = _sorted(d)
+    R = O.Rasm(g, xs, ys, zs, d["cell_start"].astype(np.int32), basic=pc == "asm", factor="chol_lu")
+    assert R.status == 0
+    n = len(d["x"])
+    r = np.random.default_rng(12).standard_normal(n)
+    perm = d["perm"]
+    ref = np.empty(n)
+    ref[perm] = R.apply(r[perm])
+    with _ctx(d, pc=pc, block_fallback="lu") as c:
+        c.matvec_setup(d["x"], d["y"], d.get("z"))
+        c.pc_setup("fp64")
+        out = c.pc_apply(r)
+        nlu = R.block_info(0)[2]
+        if case == "g2d_ragged":
+            assert nlu == 15  # the dense blob's near-singular blocks
+            cells = [cc for cc in range(len(d["cell_start"]) - 1) if d["buffer_off"][cc + 1] > d["buffer_off"][cc]]
+            refused = 0
+            for cell in cells:  # an LU-factored block has no Cholesky factor to read back
+                try:
+                    c.pc_block(cell, block=False)
+                except PrbfError as e:
+                    assert e.status == N.ERR_STATE
+                    refused += 1
+            assert refused == nlu
+    np.testing.assert_array_equal(out, ref)
+
+
+def test_lu_fallback_zero_pivot_is_the_reference_failure():
+    # five points repeated: their blocks are exactly singular. The reference's PETSc LU
+    # stops on the zero pivot; with the LU fallback the set-up fails the same way (the
+    # oracle's restatement and the reference's LU form agree), while the default shift
+    # fallback factors the blocks and solves the consistent system
+    p = W.lamb_oseen_lattice_1e4()
+    idx = np.arange(10, 15)
+    x, y = np.concatenate([p.x, p.x[idx]]), np.concatenate([p.y, p.y[idx]])
+    f = np.concatenate([p.f, p.f[idx]])
+    g = O.grid_for(x, y, None, *p.params())
+    perm, cs = O.cell_sort(g, x, y)
+    for factor in ("lu", "chol_lu"):
+        assert O.Rasm(g, x[perm], y[perm], None, cs, factor=factor).status != 0
+    assert O.Rasm(g, x[perm], y[perm], None, cs, factor="chol").status == 0
+    kw = dict(dim=2, sigma=p.sigma, nsigma_box=p.nsigma_box, sigma_buffer=p.sigma_buffer,
+              sigma_trunc=p.sigma_trunc)
+    with Context(block_fallback="lu", **kw) as c:
+        with pytest.raises(PrbfError) as e:
+            c.interpolate(x, y, None, f)
+        assert e.value.status == N.ERR_FACTOR and "zero pivot" in str(e.value)
+        # the context stays usable: the same call without the duplicates solves
+        gs, st = c.interpolate(p.x, p.y, None, p.f)
+        assert st.reason == 2 and st.nblocks_fallback == 0
+    with Context(**kw) as c:
+        _, st = c.interpolate(x, y, None, f)
+        assert st.reason == 2 and st.nblocks_fallback > 0

@@ -261,3 +261,41 @@ def test_weights_move_with_rounding_order_alone():
     assert q1 == q2 == 2
     assert 2e-11 < rel(gc2, gc1) < 5e-10
     assert rel(g1, gc1) < 1e-12  # the same arithmetic: its 1e-13 stop is already at its solution
+
+
+def test_lu_fallback_restatement(golden):
+    # the oracle's restatement of the GPU library's LU fallback: on the ragged fixture the 15
+    # blocks whose ordered Cholesky meets a non-positive pivot are factored by LU (none
+    # shifted), every other block keeps the Cholesky factor of the plain restatement; the
+    # applies are finite; exactly singular blocks (duplicated points) fail as PETSc's LU does
+    d = golden("g2d_ragged")
+    g = O.grid_for(d["x"], d["y"], None, float(d["sigma"]), int(d["nsigma_box"]), int(d["sigma_buffer"]),
+                   int(d["sigma_trunc"]))
+    perm = d["perm"]
+    xs, ys = d["x"][perm], d["y"][perm]
+    cs = d["cell_start"].astype(np.int32)
+    R1 = O.Rasm(g, xs, ys, None, cs, factor="chol")
+    R2 = O.Rasm(g, xs, ys, None, cs, factor="chol_lu")
+    assert R1.status == 0 and R2.status == 0
+    assert R1.block_info(0)[2] == 15 and R2.block_info(0)[2] == 15
+    lu_cells, same = 0, 0
+    for cell in range(len(cs) - 1):
+        if d["buffer_off"][cell + 1] == d["buffer_off"][cell]:
+            continue
+        try:
+            rows = R2.factor_rows(cell)
+        except Exception:
+            lu_cells += 1
+            continue
+        np.testing.assert_array_equal(rows, R1.factor_rows(cell))
+        same += 1
+    assert lu_cells == 15 and same > 0
+    r = np.random.default_rng(4).standard_normal(len(xs))
+    for basic in (False, True):
+        R = O.Rasm(g, xs, ys, None, cs, basic=basic, factor="chol_lu")
+        assert np.all(np.isfinite(R.apply(r)))
+    x2, y2 = np.concatenate([d["x"], d["x"][:3]]), np.concatenate([d["y"], d["y"][:3]])
+    g2 = O.grid_for(x2, y2, None, float(d["sigma"]), int(d["nsigma_box"]), int(d["sigma_buffer"]),
+                    int(d["sigma_trunc"]))
+    p2, c2 = O.cell_sort(g2, x2, y2)
+    assert O.Rasm(g2, x2[p2], y2[p2], None, c2, factor="chol_lu").status != 0
