@@ -454,6 +454,7 @@ int prbf_RBFInterpolation(int argc, char** argv, int ng, float* xg, float* yg, f
   if (eval_first && (!yp || !zp || !gp)) return PRBF_ERR_ARG;
   prbf_params p;
   prbf_params_default(&p);
+  p.block_fallback = PRBF_FALLBACK_LU;  // the reference's -sub_pc_type lu on singular blocks
   p.dim = 3;
   p.sigma = sigma;
   p.nsigma_box = nsigma_box;

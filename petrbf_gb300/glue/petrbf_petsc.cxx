@@ -20,10 +20,11 @@ PetscErrorCode lib_error(prbf_ctx* ctx, int st, const char* what) {
 }
 
 // A context with the reference's solver options (GMRES(30), rtol 1e-13, zero guess,
-// restricted Schwarz, FP64; 2d/Makefile:7).
+// restricted Schwarz, FP64, LU on the blocks the Cholesky cannot factor; 2d/Makefile:7).
 int make_ctx(int dim, double sigma, int nsigma_box, int sigma_buffer, int sigma_trunc, prbf_ctx** ctx) {
   prbf_params p;
   prbf_params_default(&p);
+  p.block_fallback = PRBF_FALLBACK_LU;
   p.dim = dim;
   p.sigma = sigma;
   p.nsigma_box = nsigma_box;
