@@ -699,6 +699,10 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   st.blo = st.bhi + 64 * TC_KCH;
   float* Ct = st.blo + 64 * TC_KCH;  // [TB][S] diagonal tile
   float* Mt = Ct + TB * S;           // [TB][S] its inverse
+  // epilogue staging of a 128 x 64 result, over the operand stage (48 KB >= 128 x 65 floats)
+  constexpr int kEtS = TB + 1;
+  static_assert(128 * kEtS <= 2 * 128 * TC_KCH + 2 * 64 * TC_KCH, "epilogue staging fits the operand stage");
+  float* Et = base;
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_abort;
@@ -752,16 +756,21 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           if (s_abort) break;
         }
         if (s_abort) break;
-        float v[32];
-        tc_load32(tmem, v);
-        const int row = pr + r_own;
-        if (row < nb)
+        // the 128 x 64 update goes through shared memory (the operand stage, idle once the
+        // MMAs have committed), so the read-modify-write of the block is row-coalesced
+        {
+          float v[32];
+          tc_load32(tmem, v);
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const int col = cbase + j;
-            // the diagonal tile keeps its lower part; rows below take the whole tile width
-            if (col < hk && (row >= rk + hk || col <= row - rk)) A[(long long)row * nb + rk + col] -= v[j];
-          }
+          for (int j = 0; j < 32; j++) Et[r_own * kEtS + cbase + j] = v[j];
+        }
+        __syncthreads();
+        for (int e = tid; e < 128 * TB; e += NTH) {
+          const int rr = e / TB, col = e % TB, row = pr + rr;
+          // the diagonal tile keeps its lower part; rows below take the whole tile width
+          if (row < nb && col < hk && (row >= rk + hk || col <= row - rk))
+            A[(long long)row * nb + rk + col] -= Et[rr * kEtS + col];
+        }
         __syncthreads();
       }
       // ---- the diagonal tile (first panel of the column): factor and invert it
@@ -797,16 +806,17 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           if (s_abort) break;
         }
         if (s_abort) break;
-        float v[32];
-        tc_load32(tmem, v);
-        const int row = pr + r_own;
-        __syncthreads();  // every thread has read its C row before any writes it over
-        if (row < nb && row >= rk + hk)
+        {
+          float v[32];
+          tc_load32(tmem, v);
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const int col = cbase + j;
-            if (col < hk) A[(long long)row * nb + rk + col] = v[j];
-          }
+          for (int j = 0; j < 32; j++) Et[r_own * kEtS + cbase + j] = v[j];
+        }
+        __syncthreads();  // every thread has read its C row and staged its result
+        for (int e = tid; e < 128 * TB; e += NTH) {
+          const int rr = e / TB, col = e % TB, row = pr + rr;
+          if (row < nb && row >= rk + hk && col < hk) A[(long long)row * nb + rk + col] = Et[rr * kEtS + col];
+        }
         __syncthreads();
       }
     }
