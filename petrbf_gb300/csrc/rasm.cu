@@ -143,20 +143,31 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
   int nc = cs[c + 1] - cs[c], n1 = nbk - nc;
   const int* id = idx + boff[c];
   T* A = K + koff[b];
+  // FP32: the block's split coordinates staged in shared memory once (block order), so an
+  // entry reads its column's coordinates from there instead of gathering them per entry
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_hl = (float2*)smem_raw;  // dim x nbk (FP32 form only)
+  if constexpr (std::is_same<T, float>::value) {
+    for (int j = threadIdx.x; j < nbk; j += blockDim.x) {
+      const int pb = id[j < n1 ? nc + j : j - n1];
+      for (int d = 0; d < dim; d++) s_hl[d * nbk + j] = hl[d * n + pb];
+    }
+    __syncthreads();
+  }
   for (int i = blockIdx.x; i < nbk; i += gridDim.x) {
     const int pa = id[i < n1 ? nc + i : i - n1];
     const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
     float2 ha[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     if constexpr (std::is_same<T, float>::value)
-      for (int d = 0; d < dim; d++) ha[d] = hl[d * n + pa];
+      for (int d = 0; d < dim; d++) ha[d] = s_hl[d * nbk + i];
     const float c2 = (float)(inv2s2 * 1.4426950408889634);
     for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-      const int pb = id[j < n1 ? nc + j : j - n1];
+      const int pb = std::is_same<T, float>::value ? 0 : id[j < n1 ? nc + j : j - n1];
       if constexpr (std::is_same<T, float>::value) {
         // differences of the split coordinates in FP32, exponent in FP32 (SFU exp2)
         float r2 = 0.f;
         for (int d = 0; d < dim; d++) {
-          const float2 hb = hl[d * n + pb];
+          const float2 hb = s_hl[d * nbk + j];
           const float dd = (ha[d].x - hb.x) + (ha[d].y - hb.y);
           r2 = fmaf(dd, dd, r2);
         }
@@ -1870,7 +1881,11 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
   const double out_scale = 2.0 * M_PI * G.sigma * G.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
   size_t smem = fp32 ? chol_smem<float>() : chol_smem<double>();
+  // FP32 assembly: the largest block's split coordinates in shared memory
+  const size_t asm_smem = fp32 ? sizeof(float2) * (size_t)G.dim * std::max(R.max_nb, 1) : 0;
   if (fp32) {
+    if (asm_smem > 200 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the assembly's shared memory");
+    PRBF_CUDA(cudaFuncSetAttribute(k_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)asm_smem));
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_tc_smem()));
   } else
@@ -1931,7 +1946,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       double shift = attempt == 0 ? 0.0 : (fp32 ? (attempt == 1 ? 1e-5 : 1e-3) : (attempt == 1 ? 1e-12 : 1e-9));
       dim3 ag(64, nb_batch);
       if (fp32) {
-        k_assemble<float><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
+        k_assemble<float><<<ag, 256, asm_smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
                                              inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n,
                                              0.0, nullptr);
         PRBF_CHECK_LAUNCH();
