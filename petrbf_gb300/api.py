@@ -209,7 +209,7 @@ class Context:
 
 
 def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="asm", device=0,
-                      precision="fp64"):
+                      precision="fp64", block_fallback="shift"):
     """Solves many independent problems together. problems: sequence of dicts with keys x,
     y, (z), f, sigma, nsigma_box, sigma_buffer, sigma_trunc. precision "mixed": FP32 sums
     and block factors inside FP64 refinement per problem. Returns (list of weight arrays,
@@ -232,7 +232,7 @@ def batch_interpolate(problems, dim=2, rtol=1e-13, restart=30, max_it=1000, pc="
     reason = np.zeros(len(probs), np.int32)
     st = N.BatchStats()
     with Context(dim=dim, rtol=rtol, restart=restart, max_it=max_it, pc=pc, device=device,
-                 precision=precision) as c:
+                 precision=precision, block_fallback=block_fallback) as c:
         code = N.lib().prbf_batch_interpolate(c.h, len(probs), arr, its.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                               reason.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                               ctypes.byref(st))

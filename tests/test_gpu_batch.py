@@ -88,3 +88,25 @@ def test_mixed_batch_meets_the_fp64_residual_and_routes_ill_conditioned_problems
     for q, gq in zip(lat, g):
         if q["meta"]["h_over_sigma"] > 0.8:
             assert _true_resid(q, gq) < 2e-13
+
+
+def test_batch_lu_fallback():
+    # block_fallback "lu": a batch without singular blocks solves exactly as with the default
+    # (no block needs a fallback); one problem with duplicated points makes the set-up fail
+    # with the reference's zero-pivot error instead of being shifted
+    from petrbf_gb300 import _native as N
+    probs = _small_batch(4, seed=5)
+    g0, its0, _, st0 = batch_interpolate(probs, rtol=1e-12, pc="asm")
+    g1, its1, _, st1 = batch_interpolate(probs, rtol=1e-12, pc="asm", block_fallback="lu")
+    assert st0.nblocks_fallback == 0 and st1.nblocks_fallback == 0
+    assert list(its0) == list(its1)
+    for a, b in zip(g0, g1):
+        np.testing.assert_array_equal(a, b)
+    q = dict(probs[1])
+    q["x"], q["y"], q["f"] = (np.concatenate([q[k], q[k][:3]]) for k in ("x", "y", "f"))
+    dup = [probs[0], q, probs[2]]
+    _, _, _, st = batch_interpolate(dup, rtol=1e-12, pc="asm")
+    assert st.nblocks_fallback > 0
+    with pytest.raises(PrbfError) as e:
+        batch_interpolate(dup, rtol=1e-12, pc="asm", block_fallback="lu")
+    assert e.value.status == N.ERR_FACTOR
