@@ -238,6 +238,23 @@ struct Chunk {
 // Rows at or past nr (the tile's height) are zero padding that is never stored: their
 // threads skip the arithmetic, whole warps where the tile ends above their 8 rows (the
 // short last tile of a block), and a partial chunk stops at mm.
+// Output mapping of a 64 x 64 tile over the 256 threads: 4 x 4 blocks (ty, tx) of the 16 x 16
+// block grid, thread 16 ty + tx; or, for a diagonal tile of the factorisation (only its
+// lower part is kept), its 136 blocks with tx <= ty on threads 0 .. 135, so that warps 5 .. 7
+// issue no arithmetic there. Each entry still receives the same operations in the same order.
+struct TileMap {
+  int ty, tx;
+  bool on;
+};
+__device__ __forceinline__ TileMap tile_map(bool lower_blocks) {
+  const int t = threadIdx.x;
+  if (!lower_blocks) return TileMap{t / 16, t % 16, true};
+  if (t >= 136) return TileMap{0, 0, false};
+  int by = 0;
+  while ((by + 1) * (by + 2) / 2 <= t) by++;  // row of block t in the lower triangle
+  return TileMap{by, t - by * (by + 1) / 2, true};
+}
+
 template <class T>
 __device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4], int ty, int tx, int nr, int mm) {
   if (4 * ty >= nr) return;
@@ -268,10 +285,11 @@ __device__ __forceinline__ void mma_chunk(const T* As, const T* Bs, T acc[4][4],
 // opB(Q)(c, m): likewise.
 template <class T>
 __device__ void tile_update(Tiles<T>& t, T acc[4][4], const T* P, long long ldp, int pr, int pc, int nr, bool ta,
-                            const T* Q, long long ldq, int qr, int qc, int ncol, bool tb, int nm) {
+                            const T* Q, long long ldq, int qr, int qc, int ncol, bool tb, int nm,
+                            TileMap mp = tile_map(false)) {
   constexpr int KC = KCOf<T>::v;
   constexpr int S = SP<T>::S;
-  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  const int ty = mp.ty, tx = mp.tx;
   const int nchunk = (nm + KC - 1) / KC;
   Chunk<T> ca, cb;
   auto fetch = [&](int m0) {
@@ -294,14 +312,15 @@ __device__ void tile_update(Tiles<T>& t, T acc[4][4], const T* P, long long ldp,
     cb.store(Bs, tb);
     __syncthreads();
     if (c + 1 < nchunk) fetch((c + 1) * KC);  // in flight during this chunk's arithmetic
-    mma_chunk<T>(As, Bs, acc, ty, tx, nr, min(KC, nm - c * KC));
+    if (mp.on) mma_chunk<T>(As, Bs, acc, ty, tx, nr, min(KC, nm - c * KC));
   }
 }
 
 template <class T>
-__device__ void acc_to_smem(T* C, const T acc[4][4]) {
+__device__ void acc_to_smem(T* C, const T acc[4][4], TileMap mp = tile_map(false)) {
   constexpr int S = SP<T>::S;
-  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  if (!mp.on) return;
+  const int ty = mp.ty, tx = mp.tx;
 #pragma unroll
   for (int p = 0; p < 4; p++)
 #pragma unroll
@@ -499,14 +518,15 @@ __device__ void store_acc(T* dst, long long ld, int r0, int c0, int nr, int nc, 
 }
 
 template <class T>
-__device__ void load_acc(const T* src, long long ld, int r0, int c0, int nr, int nc, T acc[4][4], bool lower_only) {
-  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+__device__ void load_acc(const T* src, long long ld, int r0, int c0, int nr, int nc, T acc[4][4], bool lower_only,
+                         TileMap mp = tile_map(false)) {
+  const int ty = mp.ty, tx = mp.tx;
 #pragma unroll
   for (int p = 0; p < 4; p++)
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       int r = ty * 4 + p, c = tx * 4 + q;
-      bool ok = r < nr && c < nc && (!lower_only || (r0 + r) >= (c0 + c));
+      bool ok = mp.on && r < nr && c < nc && (!lower_only || (r0 + r) >= (c0 + c));
       acc[p][q] = ok ? src[(long long)(r0 + r) * ld + c0 + c] : T(0);
     }
 }
@@ -1051,14 +1071,15 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_fp64(int nblk, const int* __res
     const int rk = k * TB, hk = min(TB, nb - rk);
     for (int i = k; i < ntile; i++) {
       const int ri = i * TB, hi = min(TB, nb - ri);
+      const TileMap mp = tile_map(i == k);  // a diagonal tile: its lower blocks only
       T acc[4][4];
-      load_acc<T>(A, nb, ri, rk, hi, hk, acc, true);
+      load_acc<T>(A, nb, ri, rk, hi, hk, acc, true, mp);
       for (int p = 0; p < k; p++) {
         const int rp = p * TB, hp = min(TB, nb - rp);
-        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, A, nb, rk, rp, hk, false, hp);
+        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, A, nb, rk, rp, hk, false, hp, mp);
       }
       __syncthreads();
-      acc_to_smem<T>(t.C, acc);
+      acc_to_smem<T>(t.C, acc, mp);  // potrf_rd zeroes the upper part it does not write
       __syncthreads();
       if (i == k) {
         ok = potrf_rd<T>(t.C, s_rd, hk) && ok;
