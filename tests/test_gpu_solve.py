@@ -246,6 +246,25 @@ def test_basic_asm_apply_matches_oracle_3d(precision, tol):
     assert _rel(out, ref) < tol
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 5e-3)])
+def test_restricted_apply_matches_oracle_3d(precision, tol):
+    # the restricted form of the factor-form applies (back substitution over the centre rows
+    # only, which start at an arbitrary row of the block): FP64 and the FP32 warp-per-block
+    # substitutions against the oracle's LU blocks
+    x, y, z, prm = _lattice3d_problem(12, 2)
+    g = O.grid_for(x, y, z, *prm)
+    perm, cs = O.cell_sort(g, x, y, z)
+    R = O.Rasm(g, x[perm], y[perm], z[perm], cs, basic=False)
+    r = np.random.default_rng(6).standard_normal(len(x))
+    ref = np.empty(len(x))
+    ref[perm] = R.apply(r[perm])
+    with Context(dim=3, sigma=prm[0], nsigma_box=2, sigma_buffer=6, sigma_trunc=16, pc="rasm") as c:
+        c.matvec_setup(x, y, z)
+        c.pc_setup(precision)
+        out = c.pc_apply(r)
+    assert _rel(out, ref) < tol
+
+
 def test_basic_asm_solve_3d_matches_oracle():
     # same Krylov path as the oracle's PETSc restatement: identical iteration counts
     x, y, z, prm = _lattice3d_problem(12, 2)
