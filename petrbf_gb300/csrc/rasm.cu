@@ -357,66 +357,6 @@ __device__ void smem_mul(const T* M, const T* C, T acc[4][4], bool left, bool tr
   }
 }
 
-// In-place Cholesky of the h x h leading part of C (lower), then its inverse into M.
-// Returns false if a pivot is not positive. Entries outside h x h are set to identity.
-template <class T>
-__device__ bool potrf_trtri(T* C, T* M, int h) {
-  constexpr int S = SP<T>::S;
-  __shared__ int s_bad;
-  if (threadIdx.x == 0) s_bad = 0;
-  __syncthreads();
-  for (int e = threadIdx.x; e < TB * TB; e += NTH) {
-    int r = e / TB, c = e % TB;
-    if (r >= h || c >= h) C[r * S + c] = (r == c) ? T(1) : T(0);
-    if (c > r) C[r * S + c] = T(0);
-  }
-  __syncthreads();
-  // each thread owns a fixed 4 x 4 sub-block (rows 4 ty .., columns 4 tx ..) of the tile
-  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-  for (int j = 0; j < h; j++) {
-    T d = C[j * S + j];
-    if (!(d > T(0))) {
-      if (threadIdx.x == 0) s_bad = 1;
-      d = T(1);
-    }
-    T s = sqrt(d);
-    __syncthreads();
-    // column j below the diagonal, then the rank-1 update of the trailing lower part
-    for (int i = j + 1 + threadIdx.x; i < h; i += NTH) C[i * S + j] /= s;
-    __syncthreads();
-    if (threadIdx.x == 0) C[j * S + j] = s;
-    T ci[4], cl[4];
-#pragma unroll
-    for (int p = 0; p < 4; p++) {
-      const int i = 4 * ty + p, l = 4 * tx + p;
-      ci[p] = (i > j && i < h) ? C[i * S + j] : T(0);
-      cl[p] = (l > j && l < h) ? C[l * S + j] : T(0);
-    }
-#pragma unroll
-    for (int p = 0; p < 4; p++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int i = 4 * ty + p, l = 4 * tx + q;
-        if (l > j && l <= i && i < h) C[i * S + l] = fma(-ci[p], cl[q], C[i * S + l]);
-      }
-    __syncthreads();
-  }
-  // M = C^-1 (lower triangular), column by column: thread c owns column c
-  for (int e = threadIdx.x; e < TB * TB; e += NTH) M[(e / TB) * S + (e % TB)] = T(0);
-  __syncthreads();
-  if (threadIdx.x < TB) {
-    int c = threadIdx.x;
-    M[c * S + c] = T(1) / C[c * S + c];
-    for (int r = c + 1; r < TB; r++) {
-      T s = T(0);
-      for (int k = c; k < r; k++) s = fma(C[r * S + k], M[k * S + c], s);
-      M[r * S + c] = -s / C[r * S + r];
-    }
-  }
-  __syncthreads();
-  return s_bad == 0;
-}
-
 // Ordered form of the diagonal-tile Cholesky (plain FP64 factor form): the h x h leading
 // part of C (lower) becomes L_kk in place, rd[j] = 1 / L_kk[j][j]. Column j: s = sqrt(c_jj),
 // r = 1/s, l_ij = c_ij * r, then c_il = fma(-l_ij, l_lj, c_il) for j < l <= i. Every entry
@@ -559,6 +499,135 @@ __host__ __device__ __forceinline__ long long rowoff(long long i) {
   return A * (A * q * (q + 1) / 2 + rr * (q + 1));
 }
 
+// ---- diagonal tiles of the tensor-core Cholesky -----------------------------------------
+// The h x h leading part of C (lower, stride S) becomes L_kk and M its inverse (lower),
+// entries outside h x h the identity (a non-positive pivot is taken as 1 and reported).
+// Warp w owns columns 8w .. 8w + 7 and lane l rows l and l + 32 of them: 16 entries per
+// thread, in registers for the whole factorisation.
+// Step j: every warp applies the published column j of L to its own columns; then the
+// owner of column j + 1, whose entries are now final, takes the pivot, scales the column
+// and publishes it into the other half of a double buffer -- one CTA barrier per column,
+// no shared-memory read-modify-write. The inverse needs no CTA barrier: forward
+// substitution L M = I by rows, each warp on its own columns, row k's eight entries
+// broadcast from their lane by shuffles. Pivots are applied as reciprocals, one IEEE
+// division per column instead of one per entry: with a division per entry the inverse
+// took eight times as long (clock64 per CTA on 900-point blocks).
+
+// The owner warp of column j (Q = j % 8) takes the pivot, scales the column and writes it to
+// buf with zeros at and above the diagonal.
+template <int Q>
+__device__ __forceinline__ void potrf_pub(float (&a)[2][8], int j, float* buf, float* rdg, int* s_bad, int h) {
+  const int lane = threadIdx.x & 31;
+  float d = __shfl_sync(0xffffffffu, j < 32 ? a[0][Q] : a[1][Q], j & 31);
+  if (!(d > 0.f)) {
+    if (lane == 0 && j < h) *s_bad = 1;
+    d = 1.f;
+  }
+  const float s = sqrtf(d), rs = 1.f / s;
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++) {
+    const int i = lane + 32 * hh;
+    float v = a[hh][Q];
+    if (i > j)
+      v *= rs;
+    else if (i == j)
+      v = s;
+    a[hh][Q] = v;
+    buf[i] = i > j ? v : 0.f;
+  }
+  if (lane == 0) rdg[j] = rs;
+}
+
+// j % 8 as a template argument (constant once the caller's loop is unrolled)
+__device__ __forceinline__ void potrf_pub_j(float (&a)[2][8], int j, float* buf, float* rdg, int* s_bad, int h) {
+  switch (j & 7) {
+    case 0: potrf_pub<0>(a, j, buf, rdg, s_bad, h); break;
+    case 1: potrf_pub<1>(a, j, buf, rdg, s_bad, h); break;
+    case 2: potrf_pub<2>(a, j, buf, rdg, s_bad, h); break;
+    case 3: potrf_pub<3>(a, j, buf, rdg, s_bad, h); break;
+    case 4: potrf_pub<4>(a, j, buf, rdg, s_bad, h); break;
+    case 5: potrf_pub<5>(a, j, buf, rdg, s_bad, h); break;
+    case 6: potrf_pub<6>(a, j, buf, rdg, s_bad, h); break;
+    default: potrf_pub<7>(a, j, buf, rdg, s_bad, h); break;
+  }
+}
+
+__device__ bool potrf_trtri_w(float* C, float* M, int h) {
+  constexpr int S = SP<float>::S;
+  static_assert(NTH == 256 && TB == 64, "eight warps of eight columns, two rows per lane");
+  __shared__ __align__(16) float colb[2][TB];
+  __shared__ float rdg[TB];  // 1 / l_jj
+  __shared__ int s_bad;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float a[2][8];
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int i = lane + 32 * hh, l = 8 * w + q;
+      a[hh][q] = (i < h && l < h) ? (l <= i ? C[i * S + l] : 0.f) : (i == l ? 1.f : 0.f);
+    }
+  if (threadIdx.x == 0) s_bad = 0;
+  if (w == 0) potrf_pub<0>(a, 0, colb[0], rdg, &s_bad, h);
+  __syncthreads();
+  for (int jb = 0; jb < TB / 8; jb++) {
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) {
+      const int j = 8 * jb + jj;
+      const float* cb = colb[j & 1];
+      const float ci[2] = {cb[lane], cb[lane + 32]};
+      const float4 c0 = *(const float4*)(cb + 8 * w), c1 = *(const float4*)(cb + 8 * w + 4);
+      const float cl[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      // zeros at and above the diagonal of column j leave rows <= j and column j as they are
+#pragma unroll
+      for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+        for (int q = 0; q < 8; q++) a[hh][q] = fma(-ci[hh], cl[q], a[hh][q]);
+      if (j + 1 < TB && w == ((j + 1) >> 3)) potrf_pub_j(a, j + 1, colb[(j + 1) & 1], rdg, &s_bad, h);
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int i = lane + 32 * hh, l = 8 * w + q;
+      C[i * S + l] = l <= i ? a[hh][q] : 0.f;
+    }
+  __syncthreads();
+  // M = L^-1: x[i][c] starts at delta_ic; row k: m_kc = x[k][c] / l_kk, then x[i][c] -= l_ik m_kc
+  // for the rows below
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[hh][q] = (lane + 32 * hh == 8 * w + q) ? 1.f : 0.f;
+  for (int k = 0; k < TB; k++) {
+    const float rkk = rdg[k];
+    const float lik[2] = {C[lane * S + k], C[(lane + 32) * S + k]};
+    const bool own0 = k < 32 && lane == k, own1 = k >= 32 && lane == k - 32;
+    float mk[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const float v = (k < 32 ? a[0][q] : a[1][q]) * rkk;  // the owner lane's value is the one kept
+      if (own0) a[0][q] = v;
+      if (own1) a[1][q] = v;
+      mk[q] = __shfl_sync(0xffffffffu, v, k & 31);
+    }
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+      if (lane + 32 * hh <= k) continue;
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[hh][q] = fma(-lik[hh], mk[q], a[hh][q]);
+    }
+  }
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) M[(lane + 32 * hh) * S + 8 * w + q] = a[hh][q];
+  __syncthreads();
+  return s_bad == 0;
+}
+
 // ---- FP32 block Cholesky on the tensor cores (tcgen05, 3xTF32) ------------------------
 // The trailing updates C_ik -= sum_p L_ip L_kp^T and the panel solves L_ik = C_ik L_kk^-T
 // of the left-looking tile Cholesky are GEMMs: each runs as tcgen05.mma kind::tf32 with
@@ -569,7 +638,7 @@ __host__ __device__ __forceinline__ long long rowoff(long long i) {
 // matrices of 8 rows x 16 bytes; element (r, k) at (r/8)*SBO + (k/4)*128 + (r%8)*16 +
 // (k%4)*4 bytes, SBO = 8 core matrices = 1024 bytes, LBO = 128 bytes). One elected thread
 // issues the MMAs and commits them to an mbarrier; the diagonal tiles are factored and
-// inverted on the CUDA cores (potrf_trtri). Writes L (lower part) over the dense block and,
+// inverted on the CUDA cores (potrf_trtri_w). Writes L (lower part) over the dense block and,
 // for the S_c form, the diagonal inverses; k_chol_sc then runs its epilogues only.
 constexpr int TC_KCH = 32;  // K columns per operand chunk
 
@@ -796,11 +865,25 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           for (int j = 0; j < 32; j++) Et[r_own * kEtS + cbase + j] = v[j];
         }
         __syncthreads();
-        for (int e = tid; e < 128 * TB; e += NTH) {
-          const int rr = e / TB, col = e % TB, row = pr + rr;
-          // the diagonal tile keeps its lower part; rows below take the whole tile width
-          if (row < nb && col < hk && (row >= rk + hk || col <= row - rk))
-            A[(long long)row * nb + rk + col] -= Et[rr * kEtS + col];
+        // the diagonal tile keeps its lower part; rows below take the whole tile width. A
+        // thread's eight loads of the block are all issued before its first store (one
+        // load latency per eight entries instead of one per entry)
+        constexpr int kRmw = 8;
+        static_assert((128 * TB) % (kRmw * NTH) == 0, "whole groups");
+        for (int e0 = 0; e0 < 128 * TB; e0 += kRmw * NTH) {
+          float a[kRmw];
+#pragma unroll
+          for (int g = 0; g < kRmw; g++) {
+            const int e = e0 + g * NTH + tid, rr = e / TB, col = e % TB, row = pr + rr;
+            const bool in = row < nb && col < hk && (row >= rk + hk || col <= row - rk);
+            a[g] = in ? A[(long long)row * nb + rk + col] : 0.f;
+          }
+#pragma unroll
+          for (int g = 0; g < kRmw; g++) {
+            const int e = e0 + g * NTH + tid, rr = e / TB, col = e % TB, row = pr + rr;
+            if (row < nb && col < hk && (row >= rk + hk || col <= row - rk))
+              A[(long long)row * nb + rk + col] = a[g] - Et[rr * kEtS + col];
+          }
         }
         __syncthreads();
       }
@@ -811,7 +894,7 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           Ct[r * S + cc] = (r < hk && cc <= r) ? A[(long long)(rk + r) * nb + rk + cc] : 0.f;
         }
         __syncthreads();
-        ok = potrf_trtri<float>(Ct, Mt, hk) && ok;
+        ok = potrf_trtri_w(Ct, Mt, hk) && ok;
         for (int e = tid; e < TB * TB; e += NTH) {
           const int r = e / TB, cc = e % TB;
           if (r < hk && cc <= r) A[(long long)(rk + r) * nb + rk + cc] = Ct[r * S + cc];
@@ -858,7 +941,9 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   if (tid == 0) bad[b] = (ok && !s_abort) ? 0 : 1;
 }
 
-// One CTA per block: Cholesky, centre columns of the inverse, S_c.
+// One CTA per block, after k_chol_tc has written L over the block (and, for S_c, the
+// diagonal tiles' inverses): the packed factor (mode 1), or the centre columns of the
+// inverse and S_c (mode 0).
 template <class T>
 __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
                                                  const long long* __restrict__ boff, const int* __restrict__ cs,
@@ -868,8 +953,7 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
                                                  double out_scale_all, const double* __restrict__ cell_sig,
                                                  unsigned char* __restrict__ bad,
                                                  const unsigned char* __restrict__ only, int mode,
-                                                 const long long* __restrict__ loff, T* __restrict__ Lpack,
-                                                 int skip_chol) {
+                                                 const long long* __restrict__ loff, T* __restrict__ Lpack) {
   int b = blockIdx.x;
   if (b >= nblk || (only && !only[b])) return;
   // per-block scale (batches of problems with their own sigma): mode 1 sqrt(1/(2 pi s^2)),
@@ -902,43 +986,7 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restr
   T* X = Xw + xoff[b];                   // nb x (nct*TB), row-major
   const long long ldx = (long long)nct * TB;
   Minv_all = X + (long long)nb * ldx;    // ntile diagonal inverses, TB x TB each
-  bool ok = true;
-  if (skip_chol) ok = bad[b] == 0;  // factored by k_chol_tc
-
-  // ---- Cholesky, left-looking over tile columns -------------------------------------
-  for (int k = 0; k < (skip_chol ? 0 : ntile); k++) {
-    int rk, hk;
-    tile_range(k, n1, nb, kc1, rk, hk);
-    for (int i = k; i < ntile; i++) {
-      int ri, hi;
-      tile_range(i, n1, nb, kc1, ri, hi);
-      T acc[4][4];
-      load_acc<T>(A, nb, ri, rk, hi, hk, acc, true);
-      for (int p = 0; p < k; p++) {
-        int rp, hp;
-        tile_range(p, n1, nb, kc1, rp, hp);
-        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, A, nb, rk, rp, hk, false, hp);
-      }
-      __syncthreads();
-      acc_to_smem<T>(t.C, acc);
-      __syncthreads();
-      if (i == k) {
-        ok = potrf_trtri<T>(t.C, t.M, hk) && ok;
-        // store L_kk (lower part) and, for the S_c phases, its inverse
-        for (int e = threadIdx.x; e < TB * TB; e += NTH) {
-          int r = e / TB, cc = e % TB;
-          if (r < hk && cc <= r) A[(long long)(rk + r) * nb + rk + cc] = t.C[r * S + cc];
-          if (mode == 0) Minv_all[(long long)k * TB * TB + e] = t.M[r * S + cc];
-        }
-        __syncthreads();
-      } else {
-        T out[4][4];
-        smem_mul<T>(t.M, t.C, out, false, false);  // C * Minv^T
-        store_acc<T>(A, nb, ri, rk, hi, hk, out);
-      }
-      __syncthreads();
-    }
-  }
+  const bool ok = bad[b] == 0;  // factored by k_chol_tc
 
   if (mode == 1) {
     // keep the factor: rows of the lower triangle, row i holding L[i][0..i], scaled so
@@ -1978,11 +2026,11 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
         if (R.factor)
           k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
                                                        (float*)Xw, R.soff.get(), nullptr, std::sqrt(1.0 / out_scale),
-                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get(), 1);
+                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get());
         else
           k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
                                                        (float*)Xw, R.soff.get(), R.S32.get(), out_scale,
-                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr, 1);
+                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr);
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
                                               G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only, nullptr, 0,

@@ -384,7 +384,9 @@ def test_edge_point_sets(precision):
     assert st.reason == 2 and st.true_rel_resid < 1e-13
     # collisions: five points repeated with the same value -- singular blocks (the reference's
     # PETSc LU stops on the zero pivot); the blocks are factored with a diagonal shift and the
-    # consistent system is still solved to the tolerance (the mixed form hands it to FP64)
+    # consistent system is still solved to the tolerance (the mixed form with its shifted FP32
+    # blocks, or in FP64 when its refinement stalls -- which of the two depends on the
+    # rounding of the FP32 factors)
     p = W.lamb_oseen_lattice_1e4()
     idx = np.arange(10, 15)
     x, y = np.concatenate([p.x, p.x[idx]]), np.concatenate([p.y, p.y[idx]])
@@ -392,7 +394,7 @@ def test_edge_point_sets(precision):
     with _ctx(p, precision=precision) as c:
         g, st = c.interpolate(x, y, None, f)
     assert st.reason == 2 and st.nblocks_fallback > 0 and st.true_rel_resid < 1e-12
-    assert st.fp64_fallback == (1 if precision == "mixed" else 0)
+    assert st.fp64_fallback in ((0, 1) if precision == "mixed" else (0,))
     # ... and with different values at the same point there is no solution: a clean error
     f2 = f.copy()
     f2[-5:] += 0.1
