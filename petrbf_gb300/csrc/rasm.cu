@@ -327,36 +327,6 @@ __device__ void acc_to_smem(T* C, const T acc[4][4], TileMap mp = tile_map(false
     for (int q = 0; q < 4; q++) C[(ty * 4 + p) * S + tx * 4 + q] = acc[p][q];
 }
 
-// out(r, c) = sum_k L(r, k) R(k, c) over smem tiles, with L = M (lower triangular) or
-// M^T when left is set, and R = C; or out = C M^T when left is false. Result in acc.
-template <class T>
-__device__ void smem_mul(const T* M, const T* C, T acc[4][4], bool left, bool transM) {
-  constexpr int S = SP<T>::S;
-  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-#pragma unroll
-  for (int p = 0; p < 4; p++)
-#pragma unroll
-    for (int q = 0; q < 4; q++) acc[p][q] = T(0);
-  for (int k = 0; k < TB; k++) {
-    T a[4], b[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      int r = ty * 4 + q, c = tx * 4 + q;
-      if (left) {
-        a[q] = transM ? M[k * S + r] : M[r * S + k];
-        b[q] = C[k * S + c];
-      } else {  // C M^T: (r, c) = sum_k C(r, k) M(c, k)
-        a[q] = C[r * S + k];
-        b[q] = M[c * S + k];
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < 4; p++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) acc[p][q] = fma(a[p], b[q], acc[p][q]);
-  }
-}
-
 // Ordered form of the diagonal-tile Cholesky (plain FP64 factor form): the h x h leading
 // part of C (lower) becomes L_kk in place, rd[j] = 1 / L_kk[j][j]. Column j: s = sqrt(c_jj),
 // r = 1/s, l_ij = c_ij * r, then c_il = fma(-l_ij, l_lj, c_il) for j < l <= i. Every entry
@@ -443,18 +413,6 @@ __device__ void trsm_rows(T* C, const T* Lk, const T* rd, int hi, int hk) {
   }
 #pragma unroll
   for (int m = 0; m < 16; m++) C[r * S + sub + 4 * m] = c[m];
-}
-
-template <class T>
-__device__ void store_acc(T* dst, long long ld, int r0, int c0, int nr, int nc, const T acc[4][4]) {
-  int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-#pragma unroll
-  for (int p = 0; p < 4; p++)
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      int r = ty * 4 + p, c = tx * 4 + q;
-      if (r < nr && c < nc) dst[(long long)(r0 + r) * ld + c0 + c] = acc[p][q];
-    }
 }
 
 template <class T>
@@ -638,8 +596,9 @@ __device__ bool potrf_trtri_w(float* C, float* M, int h) {
 // matrices of 8 rows x 16 bytes; element (r, k) at (r/8)*SBO + (k/4)*128 + (r%8)*16 +
 // (k%4)*4 bytes, SBO = 8 core matrices = 1024 bytes, LBO = 128 bytes). One elected thread
 // issues the MMAs and commits them to an mbarrier; the diagonal tiles are factored and
-// inverted on the CUDA cores (potrf_trtri_w). Writes L (lower part) over the dense block and,
-// for the S_c form, the diagonal inverses; k_chol_sc then runs its epilogues only.
+// inverted on the CUDA cores (potrf_trtri_w). Writes L (lower part) over the dense block;
+// the factor form then packs it (k_pack_factor), the restricted S_c form computes S_c in
+// the same kernel from L, L^T and the diagonal inverses (below).
 constexpr int TC_KCH = 32;  // K columns per operand chunk
 
 __device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -732,9 +691,12 @@ struct TcRegs {
   float a[16], b[8];
 };
 
+// Bsrc: the matrix the B rows come from when not from Msm (same row stride nb as A).
 __device__ __forceinline__ void tc_fetch(TcRegs& R, const float* A, int nb, int ar0, int ar_skip, int ar_end, int c0,
-                                         int c_end, int br0, int br_end, const float* Msm, int mcol0) {
+                                         int c_end, int br0, int br_end, const float* Msm, int mcol0,
+                                         const float* Bsrc = nullptr) {
   constexpr int S = SP<float>::S;
+  if (!Bsrc) Bsrc = A;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int i = 0; i < 16; i++) {  // A: core matrices w*16 + i (row group cm/8, column group cm%8)
@@ -751,7 +713,7 @@ __device__ __forceinline__ void tc_fetch(TcRegs& R, const float* A, int nb, int 
       if (Msm)
         x = Msm[r * S + mcol0 + k];
       else if (c0 + k < c_end)
-        x = A[(long long)row * nb + c0 + k];
+        x = Bsrc[(long long)row * nb + c0 + k];
     }
     R.b[i] = x;
   }
@@ -780,12 +742,71 @@ size_t chol_tc_smem() {
   return sizeof(float) * (2 * 128 * TC_KCH + 2 * 64 * TC_KCH + 2 * TB * SP<float>::S) + 64;
 }
 
+// The MMA pipeline of one 128 x 64 product: D (TMEM) = sum over the columns [k0, k1) of
+// Asrc rows [ar0, ar0 + 128) (valid in [ar_skip, ar_end)) times B^T, B the rows [br0,
+// br_end) of Bsrc or, with Msm, the rows of M in shared memory at column c - k0. Chunks of
+// 32 columns; the next chunk's loads are in flight while the tensor cores work. Returns
+// false (error flagged, s_abort set) if an MMA commit is not seen in time.
+__device__ bool tc_gemm(const TcStage& st, uint32_t tmem, uint64_t* bar, unsigned& phase, int* s_abort,
+                        unsigned* err, const float* Asrc, int ld, int ar0, int ar_skip, int ar_end, const float* Bsrc,
+                        int br0, int br_end, const float* Msm, int k0, int k1) {
+  TcRegs R;
+  tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, k0, k1, br0, br_end, Msm, 0, Bsrc);
+  for (int c0 = k0; c0 < k1; c0 += TC_KCH) {
+    tc_store(st, R);
+    tc_sync();
+    if (threadIdx.x == 0) tc_issue(tmem, st, c0 == k0);
+    if (c0 + TC_KCH < k1) tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, c0 + TC_KCH, k1, br0, br_end, Msm, c0 + TC_KCH - k0, Bsrc);
+    if (!tc_commit_wait(bar, phase)) {
+      if (threadIdx.x == 0) {
+        atomicOr(err, DEV_ERR_TIMEOUT);
+        *s_abort = 1;
+      }
+    }
+    __syncthreads();
+    if (*s_abort) return false;
+  }
+  return true;
+}
+
+// The 128 x 64 result in TMEM through shared memory (Et, over the idle operand stage) into
+// dst rows [r0, r0 + 128) below r_end, columns [c0, c0 + h): dst -= D (sub) or dst = D.
+__device__ void tc_epi(uint32_t tmem, float* Et, float* dst, long long ld, int r0, int r_end, int c0, int h, bool sub) {
+  constexpr int kEtS = TB + 1;
+  const int tid = threadIdx.x, w = tid >> 5;
+  {
+    float v[32];
+    tc_load32(tmem, v);
+    const int r_own = 32 * (w & 3) + (tid & 31), cbase = 32 * (w >> 2);
+#pragma unroll
+    for (int j = 0; j < 32; j++) Et[r_own * kEtS + cbase + j] = v[j];
+  }
+  __syncthreads();
+  constexpr int kRmw = 8;
+  for (int e0 = 0; e0 < 128 * TB; e0 += kRmw * NTH) {
+    float a[kRmw];
+#pragma unroll
+    for (int g = 0; g < kRmw; g++) {
+      const int e = e0 + g * NTH + tid, rr = e / TB, col = e % TB, row = r0 + rr;
+      a[g] = (sub && row < r_end && col < h) ? dst[(long long)row * ld + c0 + col] : 0.f;
+    }
+#pragma unroll
+    for (int g = 0; g < kRmw; g++) {
+      const int e = e0 + g * NTH + tid, rr = e / TB, col = e % TB, row = r0 + rr;
+      if (row < r_end && col < h) dst[(long long)row * ld + c0 + col] = sub ? a[g] - Et[rr * kEtS + col] : Et[rr * kEtS + col];
+    }
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restrict__ blk_cell,
                                                      const long long* __restrict__ boff, const int* __restrict__ cs,
                                                      const long long* __restrict__ koff, float* __restrict__ K,
                                                      const long long* __restrict__ xoff, float* __restrict__ Xw,
                                                      unsigned char* __restrict__ bad,
                                                      const unsigned char* __restrict__ only, int mode,
+                                                     const long long* __restrict__ soff, float* __restrict__ Sout,
+                                                     double out_scale_all, const double* __restrict__ cell_sig,
                                                      unsigned* __restrict__ err) {
   const int b = blockIdx.x;
   if (b >= nblk || (only && !only[b])) return;
@@ -815,7 +836,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   const int ntile = kc1 + (mode == 1 ? 0 : (nc + TB - 1) / TB);
   const int nct = ntile - kc1;
   float* A = K + koff[b];
-  float* Minv_all = Xw + xoff[b] + (long long)nb * nct * TB;
+  float* Minv_all = Xw + xoff[b];  // mode 0: the diagonal tiles' inverses, TB x TB each
+  (void)nct;
 
   if (tid == 0) {
     mbar_init(&bar, 1);
@@ -931,6 +953,76 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           const int rr = e / TB, col = e % TB, row = pr + rr;
           if (row < nb && row >= rk + hk && col < hk) A[(long long)row * nb + rk + col] = Et[rr * kEtS + col];
         }
+        if (mode == 0) {
+          // the same entries transposed over the upper triangle, A[rk + col][row] = L[row][rk +
+          // col], which the Cholesky never reads: the rows of L^T the S_c phase takes as B
+          for (int e = tid; e < 128 * TB; e += NTH) {
+            const int col = e / 128, rr = e % 128, row = pr + rr;
+            if (row < nb && row >= rk + hk && col < hk) A[(long long)(rk + col) * nb + row] = Et[rr * kEtS + col];
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+
+  // ---- S_c = 2 pi sigma^2 X^T, X the centre columns of K^-1 (mode 0) --------------------
+  // Z = X^T (n_c x n_b, row-major, written in place at S_c) solves Z L L^T = E_c^T, E_c the
+  // centre columns of the identity. Forward, over the centre tiles I only (Z is zero left
+  // of them): Z_I = (E_I^T - Z[:, n1..r_I) L_I,[n1..r_I)^T) M_II^T. Back, over all tiles
+  // from the last: Z_J = (Z_J - Z[:, r_J + h_J..) (L^T)_J,[r_J + h_J..)^T) M_JJ with the rows
+  // of L^T from the upper triangle. Every product is a 128-row panel of Z (128 centre
+  // points per pass) times 64 rows of L, L^T or M on the tensor cores, the same MMA pipeline
+  // as the factorisation. The centre columns are scaled once they are final; the neighbour
+  // columns, linear in them, then come out scaled.
+  if (mode == 0 && ok && !s_abort) {
+    float* Z = Sout + soff[c];
+    const float zscale = (float)(cell_sig ? 2.0 * M_PI * cell_sig[c] * cell_sig[c] : out_scale_all);
+    for (long long e = tid; e < (long long)nc * nb; e += NTH) {
+      const int n = (int)(e / nb), j = (int)(e % nb);
+      Z[e] = j == n1 + n ? 1.f : 0.f;
+    }
+    __syncthreads();
+    for (int pr = 0; pr < nc && !s_abort; pr += 128) {
+      for (int I = kc1; I < ntile && !s_abort; I++) {  // forward
+        int rI, hI;
+        tile_range(I, n1, nb, kc1, rI, hI);
+        if (rI > n1) {
+          if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, A, rI, rI + hI, nullptr, n1, rI))
+            break;
+          tc_epi(tmem, Et, Z, nb, pr, nc, rI, hI, true);
+        }
+        for (int e = tid; e < TB * TB; e += NTH) Mt[(e / TB) * S + e % TB] = Minv_all[(long long)I * TB * TB + e];
+        __syncthreads();
+        if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, nullptr, 0, hI, Mt, rI, rI + hI)) break;
+        tc_epi(tmem, Et, Z, nb, pr, nc, rI, hI, false);
+      }
+      for (int J = ntile - 1; J >= 0 && !s_abort; J--) {  // back
+        int rJ, hJ;
+        tile_range(J, n1, nb, kc1, rJ, hJ);
+        if (J == kc1 - 1) {  // the centre columns are final: scale them
+          for (int e = tid; e < 128 * nc; e += NTH) {
+            const int n = pr + e / nc, j = n1 + e % nc;
+            if (n < nc) Z[(long long)n * nb + j] *= zscale;
+          }
+          __syncthreads();
+        }
+        if (rJ + hJ < nb) {
+          if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, A, rJ, rJ + hJ, nullptr, rJ + hJ, nb))
+            break;
+          tc_epi(tmem, Et, Z, nb, pr, nc, rJ, hJ, true);
+        }
+        for (int e = tid; e < TB * TB; e += NTH)  // M_JJ^T
+          Mt[(e % TB) * S + e / TB] = Minv_all[(long long)J * TB * TB + e];
+        __syncthreads();
+        if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, nullptr, 0, hJ, Mt, rJ, rJ + hJ)) break;
+        tc_epi(tmem, Et, Z, nb, pr, nc, rJ, hJ, false);
+      }
+      if (kc1 == 0 && !s_abort) {  // no neighbour tiles: the centre columns are all of Z
+        for (int e = tid; e < 128 * nc; e += NTH) {
+          const int n = pr + e / nc, j = n1 + e % nc;
+          if (n < nc) Z[(long long)n * nb + j] *= zscale;
+        }
         __syncthreads();
       }
     }
@@ -941,140 +1033,32 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   if (tid == 0) bad[b] = (ok && !s_abort) ? 0 : 1;
 }
 
-// One CTA per block, after k_chol_tc has written L over the block (and, for S_c, the
-// diagonal tiles' inverses): the packed factor (mode 1), or the centre columns of the
-// inverse and S_c (mode 0).
-template <class T>
-__global__ void __launch_bounds__(NTH, 2) k_chol_sc(int nblk, const int* __restrict__ blk_cell,
-                                                 const long long* __restrict__ boff, const int* __restrict__ cs,
-                                                 const long long* __restrict__ koff, T* __restrict__ K,
-                                                 const long long* __restrict__ xoff, T* __restrict__ Xw,
-                                                 const long long* __restrict__ soff, T* __restrict__ Sout,
-                                                 double out_scale_all, const double* __restrict__ cell_sig,
-                                                 unsigned char* __restrict__ bad,
-                                                 const unsigned char* __restrict__ only, int mode,
-                                                 const long long* __restrict__ loff, T* __restrict__ Lpack) {
-  int b = blockIdx.x;
+// After k_chol_tc (factor form): each block's L packed by rows as the substitutions read
+// it -- row i holds L_A[i][0..i-1], then 1 / L_A[i][i] (the substitutions multiply), L_A =
+// L_K sqrt(1 / (2 pi sigma^2)) the factor of A = K / (2 pi sigma^2). One CTA per block, a
+// warp per row.
+__global__ void __launch_bounds__(NTH) k_pack_factor(int nblk, const int* __restrict__ blk_cell,
+                                                    const long long* __restrict__ boff,
+                                                    const long long* __restrict__ koff, const float* __restrict__ K,
+                                                    double scale_all, const double* __restrict__ cell_sig,
+                                                    const unsigned char* __restrict__ only,
+                                                    const long long* __restrict__ loff, float* __restrict__ Lpack) {
+  const int b = blockIdx.x;
   if (b >= nblk || (only && !only[b])) return;
-  // per-block scale (batches of problems with their own sigma): mode 1 sqrt(1/(2 pi s^2)),
-  // mode 0 2 pi s^2
-  double out_scale = out_scale_all;
-  if (cell_sig) {
-    const double sg = cell_sig[blk_cell[b]];
-    const double two_pi_s2 = 2.0 * M_PI * sg * sg;
-    out_scale = mode == 1 ? sqrt(1.0 / two_pi_s2) : two_pi_s2;
-  }
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int S = SP<T>::S;
-  constexpr int KC = KCOf<T>::v;
-  Tiles<T> t;
-  t.As = (T*)smem_raw;
-  t.Bs = t.As + 2 * KC * S;
-  t.C = t.Bs + 2 * KC * S;
-  t.M = t.C + TB * S;
-  T* Minv_all = nullptr;  // diagonal inverses live in Xw after X (see xoff layout)
-  int c = blk_cell[b];
+  const int c = blk_cell[b];
   const int nb = (int)(boff[c + 1] - boff[c]);
-  // S_c (mode 0) needs the centre columns on tile boundaries: neighbour tiles, then
-  // centre tiles. The factor form (mode 1) tiles the block uniformly, which wastes less
-  // of the 64 x 64 tile work on small blocks (two partial tiles become one).
-  const int nc = cs[c + 1] - cs[c], n1 = mode == 1 ? nb : nb - nc;
-  const int kc1 = (n1 + TB - 1) / TB;                            // neighbour (or all) tiles
-  const int ntile = kc1 + (mode == 1 ? 0 : (nc + TB - 1) / TB);  // all tiles
-  const int nct = ntile - kc1;                                   // centre tiles
-  T* A = K + koff[b];
-  T* X = Xw + xoff[b];                   // nb x (nct*TB), row-major
-  const long long ldx = (long long)nct * TB;
-  Minv_all = X + (long long)nb * ldx;    // ntile diagonal inverses, TB x TB each
-  const bool ok = bad[b] == 0;  // factored by k_chol_tc
-
-  if (mode == 1) {
-    // keep the factor: rows of the lower triangle, row i holding L[i][0..i], scaled so
-    // that it factors A = K / (2 pi sigma^2): L_A = L_K sqrt(1 / (2 pi sigma^2))
-    T* Lp = Lpack + loff[c];
-    const T sc = (T)out_scale;
-    // the diagonal is stored as its reciprocal: the substitutions then multiply
-    for (int i = 0; i < nb; i++) {
-      long long o = rowoff<T>(i);
-      for (int j = threadIdx.x; j <= i; j += NTH) {
-        T v = A[(long long)i * nb + j] * sc;
-        Lp[o + j] = j == i ? T(1) / v : v;
-      }
-    }
-    if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
-    return;
-  }
-  // ---- forward: Y = L^-1 E_centre (centre tiles only), stored in X -------------------
-  for (int i = kc1; i < ntile; i++) {
-    int ri, hi;
-    tile_range(i, n1, nb, kc1, ri, hi);
-    // diagonal inverse of tile i into M
-    for (int e = threadIdx.x; e < TB * TB; e += NTH) t.M[(e / TB) * S + e % TB] = Minv_all[(long long)i * TB * TB + e];
-    for (int cj = 0; cj < nct; cj++) {
-      int j = kc1 + cj;
-      if (j > i) break;
-      T acc[4][4];
-#pragma unroll
-      for (int p = 0; p < 4; p++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) acc[p][q] = T(0);
-      if (j == i) {
-        int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-#pragma unroll
-        for (int p = 0; p < 4; p++) acc[p][p] = (tx == ty) ? T(1) : T(0);
-      }
-      for (int p = j; p < i; p++) {  // acc -= L[i,p] Y[p, cj]
-        int rp, hp;
-        tile_range(p, n1, nb, kc1, rp, hp);
-        tile_update<T>(t, acc, A, nb, ri, rp, hi, false, X, ldx, rp, cj * TB, TB, true, hp);
-      }
-      __syncthreads();
-      acc_to_smem<T>(t.C, acc);
-      __syncthreads();
-      T out[4][4];
-      smem_mul<T>(t.M, t.C, out, true, false);  // Minv * acc
-      store_acc<T>(X, ldx, ri, cj * TB, hi, TB, out);
-      __syncthreads();
+  // per-block scale (batches of problems with their own sigma)
+  const float sc = (float)(cell_sig ? sqrt(1.0 / (2.0 * M_PI * cell_sig[c] * cell_sig[c])) : scale_all);
+  const float* A = K + koff[b];
+  float* Lp = Lpack + loff[c];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = w; i < nb; i += NTH / 32) {
+    const long long o = rowoff<float>(i);
+    for (int j = lane; j <= i; j += 32) {
+      const float v = A[(long long)i * nb + j] * sc;
+      Lp[o + j] = j == i ? 1.f / v : v;
     }
   }
-  // ---- back: X = L^-T Y, tile rows from the bottom; Y = 0 above the centre ------------
-  for (int i = ntile - 1; i >= 0; i--) {
-    int ri, hi;
-    tile_range(i, n1, nb, kc1, ri, hi);
-    for (int e = threadIdx.x; e < TB * TB; e += NTH) t.M[(e / TB) * S + e % TB] = Minv_all[(long long)i * TB * TB + e];
-    for (int cj = 0; cj < nct; cj++) {
-      T acc[4][4];
-      int cjt = kc1 + cj;
-      if (i >= kc1 && cjt <= i)
-        load_acc<T>(X, ldx, ri, cj * TB, hi, TB, acc, false);
-      else {
-#pragma unroll
-        for (int p = 0; p < 4; p++)
-#pragma unroll
-          for (int q = 0; q < 4; q++) acc[p][q] = T(0);
-      }
-      for (int j = i + 1; j < ntile; j++) {  // acc -= L[j,i]^T X[j, cj]
-        int rj, hj;
-        tile_range(j, n1, nb, kc1, rj, hj);
-        tile_update<T>(t, acc, A, nb, rj, ri, hi, true, X, ldx, rj, cj * TB, TB, true, hj);
-      }
-      __syncthreads();
-      acc_to_smem<T>(t.C, acc);
-      __syncthreads();
-      T out[4][4];
-      smem_mul<T>(t.M, t.C, out, true, true);  // Minv^T * acc
-      __syncthreads();
-      store_acc<T>(X, ldx, ri, cj * TB, hi, TB, out);
-      __syncthreads();
-    }
-  }
-  // ---- S_c[r][j] = X[j][centre col r] * out_scale, r < nc, j < nb -----------------------
-  T* Sc = Sout + soff[c];
-  for (long long e = threadIdx.x; e < (long long)nc * nb; e += NTH) {
-    int r = (int)(e / nb), j = (int)(e % nb);
-    Sc[e] = (T)((double)X[(long long)j * ldx + r] * out_scale);
-  }
-  if (threadIdx.x == 0) bad[b] = ok ? 0 : 1;
 }
 
 // ---- plain FP64 factor form: ordered block Cholesky -----------------------------------
@@ -1955,7 +1939,6 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   if (fp32) {
     if (asm_smem > 200 * 1024) throw Error(PRBF_ERR_CAPACITY, "subdomain larger than the assembly's shared memory");
     PRBF_CUDA(cudaFuncSetAttribute(k_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)asm_smem));
-    PRBF_CUDA(cudaFuncSetAttribute(k_chol_sc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_tc_smem()));
   } else
     PRBF_CUDA(cudaFuncSetAttribute(k_chol_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1991,7 +1974,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       long long n1 = nbk - nc;
       long long ntile = (n1 + TB - 1) / TB + (nc + TB - 1) / TB;
       long long nct = (nc + TB - 1) / TB;
-      long long ke = nbk * nbk, xe = R.factor ? 1 : nbk * nct * TB + ntile * TB * TB;
+      long long ke = nbk * nbk, xe = R.factor ? 1 : (fp32 ? ntile * TB * TB : nbk * nct * TB + ntile * TB * TB);
       if (!bc.empty() && (double)(hk.back() + ke + hx.back() + xe) * esz > ws_budget_bytes) break;
       if (bc.size() >= 65535) break;  // gridDim.y of the assembly
       bc.push_back(c);
@@ -2019,18 +2002,16 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
                                              inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n,
                                              0.0, nullptr);
         PRBF_CHECK_LAUNCH();
-        // the Cholesky on the tensor cores, then the factor / S_c epilogues of k_chol_sc
+        // the Cholesky on the tensor cores (and S_c), then the packed factor
         k_chol_tc<<<nb_batch, NTH, chol_tc_smem(), s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
-                                                        (float*)Xw, dbad, only, R.factor ? 1 : 0, err);
+                                                        (float*)Xw, dbad, only, R.factor ? 1 : 0, R.soff.get(),
+                                                        R.factor ? nullptr : R.S32.get(), out_scale, G.cell_sigma,
+                                                        err);
         PRBF_CHECK_LAUNCH();
         if (R.factor)
-          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
-                                                       (float*)Xw, R.soff.get(), nullptr, std::sqrt(1.0 / out_scale),
-                                                       G.cell_sigma, dbad, only, 1, R.loff.get(), R.L32.get());
-        else
-          k_chol_sc<float><<<nb_batch, NTH, smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, dk, (float*)Kw, dx,
-                                                       (float*)Xw, R.soff.get(), R.S32.get(), out_scale,
-                                                       G.cell_sigma, dbad, only, 0, nullptr, nullptr);
+          k_pack_factor<<<nb_batch, NTH, 0, s>>>(nb_batch, dbc, R.boff.get(), dk, (const float*)Kw,
+                                                  std::sqrt(1.0 / out_scale), G.cell_sigma, only, R.loff.get(),
+                                                  R.L32.get());
       } else {
         k_assemble<double><<<ag, 256, 0, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z,
                                               G.dim, inv2s2, G.cell_sigma, shift, (double*)Kw, only, nullptr, 0,
