@@ -32,6 +32,7 @@ namespace {
 
 constexpr int TB = 64;         // tile edge
 constexpr int NTH = 256;       // threads per CTA (16 x 16, 4 x 4 outputs each)
+constexpr int kAsmCtas = 16;   // CTAs per block of the assembly (a warp per row)
 static_assert(NTH == 256 && TB == 64, "the tile kernels map 16 x 16 threads onto 4 x 4 outputs each");
 // inner chunk of the tile GEMM: FP32 is latency-bound on its operand loads, so it takes
 // wider chunks; FP64 is bound by the FP64 pipe and keeps shared memory small
@@ -154,14 +155,16 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
     }
     __syncthreads();
   }
-  for (int i = blockIdx.x; i < nbk; i += gridDim.x) {
+  // a warp per row (rows dealt round-robin over the block's CTAs and warps), lanes along it
+  const int nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < nbk; i += gridDim.x * nw) {
     const int pa = id[i < n1 ? nc + i : i - n1];
     const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
     float2 ha[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     if constexpr (std::is_same<T, float>::value)
       for (int d = 0; d < dim; d++) ha[d] = s_hl[d * nbk + i];
     const float c2 = (float)(inv2s2 * 1.4426950408889634);
-    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+    for (int j = lane; j <= i; j += 32) {
       const int pb = std::is_same<T, float>::value ? 0 : id[j < n1 ? nc + j : j - n1];
       if constexpr (std::is_same<T, float>::value) {
         // differences of the split coordinates in FP32, exponent in FP32 (SFU exp2)
@@ -1996,7 +1999,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       const unsigned char* only = attempt ? dbad : nullptr;
       // diagonal shift of the retries (relative to the unit diagonal of K)
       double shift = attempt == 0 ? 0.0 : (fp32 ? (attempt == 1 ? 1e-5 : 1e-3) : (attempt == 1 ? 1e-12 : 1e-9));
-      dim3 ag(64, nb_batch);
+      dim3 ag(kAsmCtas, nb_batch);
       if (fp32) {
         k_assemble<float><<<ag, 256, asm_smem, s>>>(nb_batch, dbc, R.boff.get(), G.cs, R.idx.get(), dk, G.x, G.y, G.z, G.dim,
                                              inv2s2, G.cell_sigma, shift, (float*)Kw, only, hl, (long long)G.n,
