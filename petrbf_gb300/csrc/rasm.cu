@@ -1936,7 +1936,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
   // the diagonal inverses (ntile TB^2)
   const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
   const double out_scale = 2.0 * M_PI * G.sigma * G.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
-  size_t smem = fp32 ? chol_smem<float>() : chol_smem<double>();
+  const size_t smem = chol_smem<double>();  // the FP64 factorisation's tiles
   // FP32 assembly: the largest block's split coordinates in shared memory
   const size_t asm_smem = fp32 ? sizeof(float2) * (size_t)G.dim * std::max(R.max_nb, 1) : 0;
   if (fp32) {
