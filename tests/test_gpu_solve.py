@@ -68,6 +68,30 @@ def test_rasm_apply_matches_oracle(jitter):
     assert _rel(z32, ref) < 0.2  # FP32 factors: a preconditioner, not a solve
 
 
+@pytest.mark.parametrize("case", ["g2d_lattice100", "g2d_jitter48", "g2d_cdata", "lattice400"])
+def test_mixed_restricted_apply_tracks_fp64_blocks(golden, case):
+    # The FP32 restricted form (S_c, the centre rows of A_c^-1 from the tensor-core
+    # Cholesky and substitutions) against the FP64 factor form of the same blocks: the
+    # applies differ by the FP32 rounding of the inverses, 8e-6 to 8e-3 relative on these
+    # point sets; a wrong row, column or scale of S_c shows as O(1).
+    if case == "lattice400":
+        p = W.lamb_oseen_2d(400, jitter=0.25, seed=1)
+        dim, x, y, z, prm = 2, p.x, p.y, None, p.params()
+    else:
+        d = golden(case)
+        dim, x, y, z = int(d["dim"]), d["x"], d["y"], d.get("z")
+        prm = (float(d["sigma"]), int(d["nsigma_box"]), int(d["sigma_buffer"]), int(d["sigma_trunc"]))
+    r = np.random.default_rng(3).standard_normal(len(x))
+    with Context(dim=dim, sigma=prm[0], nsigma_box=prm[1], sigma_buffer=prm[2], sigma_trunc=prm[3], pc="rasm") as c:
+        c.matvec_setup(x, y, z)
+        c.pc_setup("fp64")
+        z64 = c.pc_apply(r)
+        c.pc_setup("mixed")
+        z32 = c.pc_apply(r)
+    assert np.all(np.isfinite(z32))
+    assert _rel(z32, z64) < 0.03
+
+
 def test_solve_lamb_oseen_lattice_1e4_fp64_converged_weights_match_oracle():
     p = W.lamb_oseen_lattice_1e4()
     go, its_o, reason_o = O.rbf_interpolation(p.x, p.y, None, p.f, *p.params(), rtol=1e-16,
