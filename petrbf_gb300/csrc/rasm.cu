@@ -601,7 +601,7 @@ __device__ bool potrf_trtri_w(float* C, float* M, int h) {
 // issues the MMAs and commits them to an mbarrier; the diagonal tiles are factored and
 // inverted on the CUDA cores (potrf_trtri_w). Writes L (lower part) over the dense block;
 // the factor form then packs it (k_pack_factor), the restricted S_c form computes S_c in
-// the same kernel from L, L^T and the diagonal inverses (below).
+// the same kernel from L and the diagonal inverses (below).
 constexpr int TC_KCH = 32;  // K columns per operand chunk
 
 __device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -694,10 +694,12 @@ struct TcRegs {
   float a[16], b[8];
 };
 
-// Bsrc: the matrix the B rows come from when not from Msm (same row stride nb as A).
+// Bsrc: the matrix the B rows come from when not from Msm (same row stride nb as A); bt:
+// B is the transpose of Bsrc, element (r, k) at Bsrc[(c0 + k) nb + br0 + r] (a warp
+// instruction then reads 4 rows of Bsrc, 32 contiguous bytes each).
 __device__ __forceinline__ void tc_fetch(TcRegs& R, const float* A, int nb, int ar0, int ar_skip, int ar_end, int c0,
                                          int c_end, int br0, int br_end, const float* Msm, int mcol0,
-                                         const float* Bsrc = nullptr) {
+                                         const float* Bsrc = nullptr, bool bt = false) {
   constexpr int S = SP<float>::S;
   if (!Bsrc) Bsrc = A;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -716,7 +718,7 @@ __device__ __forceinline__ void tc_fetch(TcRegs& R, const float* A, int nb, int 
       if (Msm)
         x = Msm[r * S + mcol0 + k];
       else if (c0 + k < c_end)
-        x = Bsrc[(long long)row * nb + c0 + k];
+        x = bt ? Bsrc[(long long)(c0 + k) * nb + row] : Bsrc[(long long)row * nb + c0 + k];
     }
     R.b[i] = x;
   }
@@ -747,19 +749,20 @@ size_t chol_tc_smem() {
 
 // The MMA pipeline of one 128 x 64 product: D (TMEM) = sum over the columns [k0, k1) of
 // Asrc rows [ar0, ar0 + 128) (valid in [ar_skip, ar_end)) times B^T, B the rows [br0,
-// br_end) of Bsrc or, with Msm, the rows of M in shared memory at column c - k0. Chunks of
-// 32 columns; the next chunk's loads are in flight while the tensor cores work. Returns
-// false (error flagged, s_abort set) if an MMA commit is not seen in time.
+// br_end) of Bsrc (of its transpose with bt) or, with Msm, the rows of M in shared memory at
+// column c - k0. Chunks of 32 columns; the next chunk's loads are in flight while the tensor
+// cores work. Returns false (error flagged, s_abort set) if an MMA commit is not seen in time.
 __device__ bool tc_gemm(const TcStage& st, uint32_t tmem, uint64_t* bar, unsigned& phase, int* s_abort,
                         unsigned* err, const float* Asrc, int ld, int ar0, int ar_skip, int ar_end, const float* Bsrc,
-                        int br0, int br_end, const float* Msm, int k0, int k1) {
+                        int br0, int br_end, const float* Msm, int k0, int k1, bool bt = false) {
   TcRegs R;
-  tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, k0, k1, br0, br_end, Msm, 0, Bsrc);
+  tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, k0, k1, br0, br_end, Msm, 0, Bsrc, bt);
   for (int c0 = k0; c0 < k1; c0 += TC_KCH) {
     tc_store(st, R);
     tc_sync();
     if (threadIdx.x == 0) tc_issue(tmem, st, c0 == k0);
-    if (c0 + TC_KCH < k1) tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, c0 + TC_KCH, k1, br0, br_end, Msm, c0 + TC_KCH - k0, Bsrc);
+    if (c0 + TC_KCH < k1)
+      tc_fetch(R, Asrc, ld, ar0, ar_skip, ar_end, c0 + TC_KCH, k1, br0, br_end, Msm, c0 + TC_KCH - k0, Bsrc, bt);
     if (!tc_commit_wait(bar, phase)) {
       if (threadIdx.x == 0) {
         atomicOr(err, DEV_ERR_TIMEOUT);
@@ -956,14 +959,6 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           const int rr = e / TB, col = e % TB, row = pr + rr;
           if (row < nb && row >= rk + hk && col < hk) A[(long long)row * nb + rk + col] = Et[rr * kEtS + col];
         }
-        if (mode == 0) {
-          // the same entries transposed over the upper triangle, A[rk + col][row] = L[row][rk +
-          // col], which the Cholesky never reads: the rows of L^T the S_c phase takes as B
-          for (int e = tid; e < 128 * TB; e += NTH) {
-            const int col = e / 128, rr = e % 128, row = pr + rr;
-            if (row < nb && row >= rk + hk && col < hk) A[(long long)(rk + col) * nb + row] = Et[rr * kEtS + col];
-          }
-        }
         __syncthreads();
       }
     }
@@ -974,8 +969,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   // centre columns of the identity. Forward, over the centre tiles I only (Z is zero left
   // of them): Z_I = (E_I^T - Z[:, n1..r_I) L_I,[n1..r_I)^T) M_II^T. Back, over all tiles
   // from the last: Z_J = (Z_J - Z[:, r_J + h_J..) (L^T)_J,[r_J + h_J..)^T) M_JJ with the rows
-  // of L^T from the upper triangle. Every product is a 128-row panel of Z (128 centre
-  // points per pass) times 64 rows of L, L^T or M on the tensor cores, the same MMA pipeline
+  // of L^T read as columns of L (transposed fetch). Every product is a 128-row panel of Z (128
+  // centre points per pass) times 64 rows of L, L^T or M on the tensor cores, the same MMA pipeline
   // as the factorisation. The centre columns are scaled once they are final; the neighbour
   // columns, linear in them, then come out scaled.
   if (mode == 0 && ok && !s_abort) {
@@ -1011,7 +1006,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
           __syncthreads();
         }
         if (rJ + hJ < nb) {
-          if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, A, rJ, rJ + hJ, nullptr, rJ + hJ, nb))
+          if (!tc_gemm(st, tmem, &bar, phase, &s_abort, err, Z, nb, pr, pr, nc, A, rJ, rJ + hJ, nullptr, rJ + hJ, nb,
+                       true))
             break;
           tc_epi(tmem, Et, Z, nb, pr, nc, rJ, hJ, true);
         }
