@@ -68,14 +68,18 @@ def test_rasm_apply_matches_oracle(jitter):
     assert _rel(z32, ref) < 0.2  # FP32 factors: a preconditioner, not a solve
 
 
-@pytest.mark.parametrize("case", ["g2d_lattice100", "g2d_jitter48", "g2d_cdata", "lattice400"])
+@pytest.mark.parametrize("case", ["g2d_lattice100", "g2d_jitter48", "g2d_cdata", "lattice400", "cells225"])
 def test_mixed_restricted_apply_tracks_fp64_blocks(golden, case):
     # The FP32 restricted form (S_c, the centre rows of A_c^-1 from the tensor-core
     # Cholesky and substitutions) against the FP64 factor form of the same blocks: the
     # applies differ by the FP32 rounding of the inverses, 8e-6 to 8e-3 relative on these
-    # point sets; a wrong row, column or scale of S_c shows as O(1).
+    # point sets; a wrong row, column or scale of S_c shows as O(1). cells225: 15 x 15 points
+    # per cell, so S_c is computed in two 128-row panels of centre points.
     if case == "lattice400":
         p = W.lamb_oseen_2d(400, jitter=0.25, seed=1)
+        dim, x, y, z, prm = 2, p.x, p.y, None, p.params()
+    elif case == "cells225":
+        p = W.lamb_oseen_2d(150, jitter=0.25, seed=2, nsigma_box=12)
         dim, x, y, z, prm = 2, p.x, p.y, None, p.params()
     else:
         d = golden(case)
