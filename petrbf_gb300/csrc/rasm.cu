@@ -557,28 +557,42 @@ __device__ bool potrf_trtri_w(float* C, float* M, int h) {
     }
   __syncthreads();
   // M = L^-1: x[i][c] starts at delta_ic; row k: m_kc = x[k][c] / l_kk, then x[i][c] -= l_ik m_kc
-  // for the rows below
+  // for the rows below. Rows above a warp's first column give m_kc = 0 for all its columns, so
+  // the warp starts at row 8w; rows 0..31 live in the lanes' first half, 32..63 in the second.
 #pragma unroll
   for (int hh = 0; hh < 2; hh++)
 #pragma unroll
     for (int q = 0; q < 8; q++) a[hh][q] = (lane + 32 * hh == 8 * w + q) ? 1.f : 0.f;
-  for (int k = 0; k < TB; k++) {
+  for (int k = 8 * w; k < 32; k++) {  // pivot row in the first half: every second-half row updates
     const float rkk = rdg[k];
-    const float lik[2] = {C[lane * S + k], C[(lane + 32) * S + k]};
-    const bool own0 = k < 32 && lane == k, own1 = k >= 32 && lane == k - 32;
+    const float lik0 = C[lane * S + k], lik1 = C[(lane + 32) * S + k];
     float mk[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-      const float v = (k < 32 ? a[0][q] : a[1][q]) * rkk;  // the owner lane's value is the one kept
-      if (own0) a[0][q] = v;
-      if (own1) a[1][q] = v;
-      mk[q] = __shfl_sync(0xffffffffu, v, k & 31);
+      const float v = a[0][q] * rkk;  // the owner lane's value is the one kept
+      if (lane == k) a[0][q] = v;
+      mk[q] = __shfl_sync(0xffffffffu, v, k);
+    }
+    if (lane > k) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[0][q] = fma(-lik0, mk[q], a[0][q]);
     }
 #pragma unroll
-    for (int hh = 0; hh < 2; hh++) {
-      if (lane + 32 * hh <= k) continue;
+    for (int q = 0; q < 8; q++) a[1][q] = fma(-lik1, mk[q], a[1][q]);
+  }
+  for (int k = max(32, 8 * w); k < TB; k++) {  // pivot row in the second half
+    const float rkk = rdg[k];
+    const float lik1 = C[(lane + 32) * S + k];
+    float mk[8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) a[hh][q] = fma(-lik[hh], mk[q], a[hh][q]);
+    for (int q = 0; q < 8; q++) {
+      const float v = a[1][q] * rkk;
+      if (lane == k - 32) a[1][q] = v;
+      mk[q] = __shfl_sync(0xffffffffu, v, k - 32);
+    }
+    if (lane + 32 > k) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[1][q] = fma(-lik1, mk[q], a[1][q]);
     }
   }
 #pragma unroll
