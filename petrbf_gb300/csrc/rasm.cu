@@ -127,6 +127,33 @@ __global__ void k_split_hl(long long n, const double* __restrict__ v, float2* __
 // the differences as the reference forms them (x_a - x_b), |d|^2 = fma(dy, dy, dx dx)
 // (+ fma(dz, dz, .)), and the exponential of the sums' table (exp_neg_tab, kexp = 1024 /
 // (2 sigma^2 ln2)), every operation rounded as written.
+// FP32 rows of the block assembly: one warp, lanes along row i (columns 0..i), the split
+// coordinates from shared memory, the exponential as the FP32 sums take it (ex2.approx);
+// the diagonal shift is added by the lane that wrote the diagonal.
+__device__ __forceinline__ float asm_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+template <int DIM>
+__device__ __forceinline__ void asm_row_f32(float* __restrict__ Arow, const float2* s_hl, int nbk, int i, float c2,
+                                            float sh, int lane) {
+  float2 ha[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; d++) ha[d] = s_hl[d * nbk + i];
+  for (int j = lane; j <= i; j += 32) {
+    float r2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const float2 hb = s_hl[d * nbk + j];
+      const float dd = (ha[d].x - hb.x) + (ha[d].y - hb.y);
+      r2 = fmaf(dd, dd, r2);
+    }
+    Arow[j] = asm_ex2(-r2 * c2);
+  }
+  if (sh != 0.f && lane == (i & 31)) Arow[i] += sh;
+}
+
 template <class T>
 __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const long long* __restrict__ boff,
                            const int* __restrict__ cs, const int* __restrict__ idx,
@@ -157,27 +184,20 @@ __global__ void k_assemble(int nblk, const int* __restrict__ blk_cell, const lon
   }
   // a warp per row (rows dealt round-robin over the block's CTAs and warps), lanes along it
   const int nw = blockDim.x >> 5, lane = threadIdx.x & 31;
-  for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < nbk; i += gridDim.x * nw) {
-    const int pa = id[i < n1 ? nc + i : i - n1];
-    const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
-    float2 ha[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    if constexpr (std::is_same<T, float>::value)
-      for (int d = 0; d < dim; d++) ha[d] = s_hl[d * nbk + i];
-    const float c2 = (float)(inv2s2 * 1.4426950408889634);
-    for (int j = lane; j <= i; j += 32) {
-      const int pb = std::is_same<T, float>::value ? 0 : id[j < n1 ? nc + j : j - n1];
-      if constexpr (std::is_same<T, float>::value) {
-        // differences of the split coordinates in FP32, exponent in FP32 (SFU exp2)
-        float r2 = 0.f;
-        for (int d = 0; d < dim; d++) {
-          const float2 hb = s_hl[d * nbk + j];
-          const float dd = (ha[d].x - hb.x) + (ha[d].y - hb.y);
-          r2 = fmaf(dd, dd, r2);
-        }
-        float v = exp2f(-r2 * c2);
-        if (i == j) v += (float)shift;
-        A[(long long)i * nbk + j] = v;
-      } else {
+  if constexpr (std::is_same<T, float>::value) {
+    const float c2 = (float)(inv2s2 * 1.4426950408889634), sh = (float)shift;
+    for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < nbk; i += gridDim.x * nw) {
+      if (dim == 3)
+        asm_row_f32<3>(A + (long long)i * nbk, s_hl, nbk, i, c2, sh, lane);
+      else
+        asm_row_f32<2>(A + (long long)i * nbk, s_hl, nbk, i, c2, sh, lane);
+    }
+  } else {
+    for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < nbk; i += gridDim.x * nw) {
+      const int pa = id[i < n1 ? nc + i : i - n1];
+      const double xa = x[pa], ya = y[pa], za = dim == 3 ? z[pa] : 0.0;
+      for (int j = lane; j <= i; j += 32) {
+        const int pb = id[j < n1 ? nc + j : j - n1];
         const double dx = __dsub_rn(xa, x[pb]), dy = __dsub_rn(ya, y[pb]);
         double r2 = __fma_rn(dy, dy, __dmul_rn(dx, dx));
         if (dim == 3) {
