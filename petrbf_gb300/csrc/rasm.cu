@@ -1010,9 +1010,9 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
   if (mode == 0 && ok && !s_abort) {
     float* Z = Sout + soff[c];
     const float zscale = (float)(cell_sig ? 2.0 * M_PI * cell_sig[c] * cell_sig[c] : out_scale_all);
-    for (long long e = tid; e < (long long)nc * nb; e += NTH) {
-      const int n = (int)(e / nb), j = (int)(e % nb);
-      Z[e] = j == n1 + n ? 1.f : 0.f;
+    for (int n = w; n < nc; n += NTH / 32) {  // a warp per row of Z
+      float* zr = Z + (long long)n * nb;
+      for (int j = tid & 31; j < nb; j += 32) zr[j] = j == n1 + n ? 1.f : 0.f;
     }
     __syncthreads();
     for (int pr = 0; pr < nc && !s_abort; pr += 128) {
@@ -1033,10 +1033,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
         int rJ, hJ;
         tile_range(J, n1, nb, kc1, rJ, hJ);
         if (J == kc1 - 1) {  // the centre columns are final: scale them
-          for (int e = tid; e < 128 * nc; e += NTH) {
-            const int n = pr + e / nc, j = n1 + e % nc;
-            if (n < nc) Z[(long long)n * nb + j] *= zscale;
-          }
+          for (int n = pr + w; n < min(pr + 128, nc); n += NTH / 32)
+            for (int j = n1 + (tid & 31); j < nb; j += 32) Z[(long long)n * nb + j] *= zscale;
           __syncthreads();
         }
         if (rJ + hJ < nb) {
@@ -1052,10 +1050,8 @@ __global__ void __launch_bounds__(NTH, 2) k_chol_tc(int nblk, const int* __restr
         tc_epi(tmem, Et, Z, nb, pr, nc, rJ, hJ, false);
       }
       if (kc1 == 0 && !s_abort) {  // no neighbour tiles: the centre columns are all of Z
-        for (int e = tid; e < 128 * nc; e += NTH) {
-          const int n = pr + e / nc, j = n1 + e % nc;
-          if (n < nc) Z[(long long)n * nb + j] *= zscale;
-        }
+        for (int n = pr + w; n < min(pr + 128, nc); n += NTH / 32)
+          for (int j = n1 + (tid & 31); j < nb; j += 32) Z[(long long)n * nb + j] *= zscale;
         __syncthreads();
       }
     }
