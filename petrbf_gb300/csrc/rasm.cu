@@ -14,13 +14,15 @@
 // true residual near 1e-11 on the 2D configurations. Mixed form: S_c = the n_c centre
 // rows of A_c^-1 (n_c x n_b, FP32) once, so an apply is one batched GEMV that streams
 // S_c from HBM; the outer FP64 refinement removes its error. Per block (one CTA):
-//   order the block neighbours first, centre last; K = A_c (2 pi sigma^2) in (0, 1];
-//   left-looking tiled Cholesky K = L L^T (64 x 64 tiles, register-tiled GEMM updates,
-//   each diagonal tile factored and inverted in shared memory);
-//   Y = L^-1 E_centre (only the centre tiles are non-zero);  X = L^-T Y = K^-1 E_centre;
-//   S_c = X^T / (2 pi sigma^2), stored row-major in the block's column order.
-// FP64 for the plain form, FP32 for the mixed form (with a diagonal-shift retry for
-// blocks whose FP32 factorisation meets a non-positive pivot).
+//   order the block neighbours first, centre last; K = 2 pi sigma^2 A_c, entries in (0, 1];
+//   left-looking tiled Cholesky K = L L^T over 64-column tiles -- FP64: k_chol_fp64 on the
+//   CUDA cores, in an operation order a CPU restatement reproduces bit for bit; FP32:
+//   k_chol_tc, updates and panel solves on the tensor cores;
+//   FP32 restricted form: S_c = 2 pi sigma^2 X^T with X = K^-1 E_centre, from Z = X^T solving
+//   Z L L^T = E_centre^T by substitutions on the tensor cores in the same kernel, stored
+//   row-major in the block's column order.
+// Blocks whose factorisation meets a non-positive pivot are retried with a diagonal shift,
+// or (FP64, on request) factored by LU with partial pivoting.
 #include <algorithm>
 #include <cmath>
 #include <vector>
