@@ -1960,8 +1960,8 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
     R.S32.reserve(std::max<long long>(hso[ncell], 1));
   }
 
-  // batches of blocks within the workspace budget: K (nb^2), X (nb x ceil(nc/TB)TB) and
-  // the diagonal inverses (ntile TB^2)
+  // batches of blocks within the workspace budget: K (nb^2) and, for the S_c form, the
+  // diagonal tiles' inverses (ntile TB^2)
   const double inv2s2 = 1.0 / (2.0 * G.sigma * G.sigma);
   const double out_scale = 2.0 * M_PI * G.sigma * G.sigma;  // A = K/(2 pi sigma^2): A^-1 = 2 pi sigma^2 K^-1
   const size_t smem = chol_smem<double>();  // the FP64 factorisation's tiles
@@ -2004,8 +2004,7 @@ void rasm_factor(RasmPlan& R, const BlockGeom& G, const std::vector<int>& hcnt, 
       long long nbk = hcnt[c], nc = hcs[c + 1] - hcs[c];
       long long n1 = nbk - nc;
       long long ntile = (n1 + TB - 1) / TB + (nc + TB - 1) / TB;
-      long long nct = (nc + TB - 1) / TB;
-      long long ke = nbk * nbk, xe = R.factor ? 1 : (fp32 ? ntile * TB * TB : nbk * nct * TB + ntile * TB * TB);
+      long long ke = nbk * nbk, xe = R.factor ? 1 : ntile * TB * TB;  // S_c form: FP32 only
       if (!bc.empty() && (double)(hk.back() + ke + hx.back() + xe) * esz > ws_budget_bytes) break;
       if (bc.size() >= 65535) break;  // gridDim.y of the assembly
       bc.push_back(c);
